@@ -1,0 +1,385 @@
+"""Benchmark of the plain SPH step at 1,048,576 particles (the dam break the solver is measured
+on), printing one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload dam1m|dam16k]
+
+value      particle-steps/s of K graph-launched steps, inputs resident in HBM, device time from
+           CUDA events around each step; L2 is flushed (a read of twice its size) before every
+           timed step, outside the timed span.
+e2e        the same metric through the C ABI with host buffers: each step uploads the particle
+           state from pinned host memory, runs update(), and reads the state back.
+roofline   the dominant kernel's algorithmic bytes per launch / its CUDA-event time, against the
+           measured HBM copy bandwidth; `traffic` is its DRAM bytes per launch from ncu
+           (profiles/ncu_traffic.json).
+cpu_baseline  the CPU transcription of the reference's stages (oracle, FP32) on this host's
+           cores, on a bounded sample of the same workload.
+--impl reference  times the reference's own shader code compiled for the host CPU
+           (oracle/_ref, when built) or else the oracle's transcription, all threads.
+Multi-GPU (torchrun): every rank runs an independent replica (the path has no exchange step);
+the slowest rank's time is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "particle-steps/s at 1M particles (plain SPH step)"
+UNIT = "particle-steps/s"
+
+WORKLOADS = {
+    # name: (particles, dt, description)
+    "dam1m": (1048576, 2.5e-4, "dam break, 1,048,576 particles, h=0.011425, 87^3 cells, dt=2.5e-4"),
+    "dam16k": (16384, 1e-3, "dam break, 16,384 particles, h=0.0457, 21^3 cells, dt=1e-3"),
+}
+
+# Algorithmic bytes per particle per launch (reads + writes the kernel must make once).
+ALGO_BYTES = {
+    "bin_count": 16.0,  # read position 12, write key 4
+    "scan_cells": None,  # per cell: read count 4, write start 4, clear count 4 (x C/N)
+    "scatter_cells": 12.0,  # read key 4 + rank 4, write slot 4
+    "rank_gather": 40.0,  # read position 12 + velocity 12 (+ key), write 24 + permutation 4
+    "density": 20.0,  # read position 12, write density + pressure 8
+    "force_integrate": 56.0,  # read position, velocity, density, pressure 32, write position, velocity 24
+}
+
+
+def step_algo_bytes(n: int, cells: int) -> float:
+    """Per particle-step algorithmic bytes of the whole step: 152 + 32 C/N (binning 16,
+    histogram 4, reorder 56, density 20, force 56, cell tables 32 per cell)."""
+    return 152.0 + 32.0 * cells / max(n, 1)
+
+
+def measured_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.is_file():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    p = REPO / "profiles" / "ncu_traffic.json"
+    if not p.is_file():
+        return None
+    d = json.loads(p.read_text())
+    e = d.get(workload, {}).get(kernel)
+    return None if e is None else float(e)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"wc_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.is_file():
+            return None
+        rows = [r.split(",") for r in self.path.read_text().strip().splitlines() if r.strip()]
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(gpus: int):
+    """(rank, world, local_rank, reduce_max) for torchrun launches; plain values for N=1."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return 0, 1, 0, (lambda x: x), (lambda: None)
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+
+    def reduce_max(x: float) -> float:
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if backend == "nccl" else "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return rank, world, local, reduce_max, dist.barrier
+
+
+def cpu_baseline(p, state, dt, threads_all: int):
+    """The oracle's FP32 transcription on a bounded sample: 2 steps on all threads, 1 step on
+    one thread, of the full workload."""
+    from oracle.oracle import Oracle
+
+    o = Oracle()
+    n = state.shape[0]
+    s = state.copy()
+    o.step(p, s, dt, 1, threads=threads_all)  # warm-up (page-in, thread pool)
+    t = time.perf_counter()
+    o.step(p, s, dt, 2, threads=threads_all)
+    t_all = (time.perf_counter() - t) / 2
+    t = time.perf_counter()
+    o.step(p, s, dt, 1, threads=1)
+    t_one = time.perf_counter() - t
+    return {
+        "value": n / t_all,
+        "unit": UNIT,
+        "cores": threads_all,
+        "kind": "port",
+        "sample": f"2 full steps (all threads) + 1 step (1 thread) of the {n}-particle workload, FP32 oracle",
+        "value_1thread": n / t_one,
+        "ms_per_step": t_all * 1e3,
+        "ms_per_step_1thread": t_one * 1e3,
+    }
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU implementation of the path on this host."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle.oracle import Oracle, RefLib, build_ref, ref_available
+    from watercube_gb300.fluid import dam_break_params, finalize, generate_dam_break
+
+    n, dt, desc = WORKLOADS[args.workload]
+    p = finalize(dam_break_params(n))
+    st = generate_dam_break(p, 0)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    try:
+        if not ref_available():
+            build_ref()
+        if ref_available():
+            kind = "reference"
+    except Exception:
+        kind = "port"
+    if kind == "reference":
+        ref = RefLib()
+        state = st.copy()
+
+        def one_step():
+            ref.step(p, state, dt, 1, threads=threads)
+    else:
+        o = Oracle()
+        state = st.copy()
+
+        def one_step():
+            o.step(p, state, dt, 1, threads=threads)
+
+    for _ in range(args.warmup):
+        one_step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    el = time.perf_counter() - t
+    value = n * args.steps / el
+    what = ("the reference's compute shaders (assets/sort/*.comp, assets/fluid/density.comp, update.comp) compiled "
+            "as C++ and dispatched in Fluid::update order, OpenMP over invocations" if kind == "reference" else
+            "the oracle's FP32 transcription of the reference's shader stages, OpenMP")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": desc, "particles": n, "grid_res": int(p.grid_res), "dt": dt},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"{args.steps} full steps of the {n}-particle workload: {what}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    rank, world, local, reduce_max, barrier = dist_setup(args.gpus)
+    from watercube_gb300 import _abi
+    from watercube_gb300.fluid import Fluid, PinnedBuffer, dam_break_params, finalize, generate_dam_break
+
+    _abi.check(_abi.lib().wc_set_device(local), "select device")
+    n, dt, desc = WORKLOADS[args.workload]
+    p = finalize(dam_break_params(n))
+    st = generate_dam_break(p, rank)
+    cells = int(p.grid_res) ** 3
+    f = Fluid.create("bench", p)
+    f.setup(st)
+    # warm-up: graph capture, clocks up
+    f.step(dt, max(args.warmup, 3))
+    f.synchronize()
+
+    barrier()
+    clocks = Clocks(local)
+    with clocks:
+        step_ms, _ = f.time_steps(dt, args.steps, flush_l2=True, kernel_times=False)
+    barrier()
+    total_ms = reduce_max(float(step_ms.sum()))
+    clock_summary = clocks.summary()
+    value = world * n * args.steps / (total_ms * 1e-3)
+
+    # per-kernel CUDA-event times (separate launches of the same steps, L2 flushed before each)
+    _, kern = f.time_steps(dt, args.steps, flush_l2=True, kernel_times=True)
+    names = Fluid.kernel_names()
+    kmean = {k: float(np.mean(kern[:, i])) for i, k in enumerate(names)}
+    dom = max(kmean, key=kmean.get)
+    peak, peak_kind = measured_peaks()
+    algo = ALGO_BYTES[dom] * n if ALGO_BYTES.get(dom) else 12.0 * cells
+    achieved = algo / (kmean[dom] * 1e-3) / 1e9
+    step_mean_ms = total_ms / args.steps
+    step_gbs = step_algo_bytes(n, cells) * n / (step_mean_ms * 1e-3) / 1e9
+
+    # end to end through the C ABI with host buffers
+    nbytes = n * 32
+    hin = PinnedBuffer(nbytes)
+    hout = PinnedBuffer(nbytes)
+    ain = hin.particles(n)
+    aout = hout.particles(n)
+    ain[:] = f.particles()
+    lib = _abi.lib()
+    e2e_steps = max(5, min(args.steps, 50))
+
+    def e2e_step(src, dst):
+        _abi.check(lib.wc_fluid_set_particles(f._handle, _abi.WC_BUFFER_STATE, src.ctypes.data, n))
+        _abi.check(lib.wc_fluid_update(f._handle, dt / float(p.time_scale)))
+        _abi.check(lib.wc_fluid_get_particles(f._handle, _abi.WC_BUFFER_STATE, dst.ctypes.data, n))
+
+    for _ in range(2):
+        e2e_step(ain, aout)
+        ain, aout = aout, ain
+    barrier()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step(ain, aout)
+        ain, aout = aout, ain
+    el = reduce_max(time.perf_counter() - t)
+    e2e_value = world * n * e2e_steps / el
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_mean_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": desc,
+            "particles_per_gpu": n,
+            "grid_res": int(p.grid_res),
+            "cells": cells,
+            "dt": dt,
+            "l2": "flushed before every timed step (read of 2x L2), outside the timed span",
+            "parallelism": f"{world} independent replicas" if world > 1 else "1 GPU",
+        },
+        "roofline": {
+            "bound": "hbm",
+            "kernel": dom,
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "algorithmic_bytes_per_launch": algo,
+            "traffic": ncu_traffic(dom, args.workload),
+            "step": {"algorithmic_bytes_per_particle": step_algo_bytes(n, cells), "achieved": step_gbs,
+                     "frac": step_gbs / peak},
+        },
+        "kernels_ms": kmean,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps,
+                "pattern": "wc_fluid_set_particles(pinned host) + wc_fluid_update + wc_fluid_get_particles(pinned host)"},
+        "gpu_launches": 6 * args.steps,
+        "clocks": clock_summary,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(p, st, dt, os.cpu_count() or 1)
+    f.close()
+    hin.free()
+    hout.free()
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="dam1m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

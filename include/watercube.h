@@ -1,0 +1,265 @@
+/*
+ * watercube.h — C ABI of the GB300 SPH water solver.
+ *
+ * This is the drop-in boundary for WaterCube's simulation path. The reference exposes it as the
+ * C++ class core::Fluid (src/core/Fluid.h:32-141) driving the GLSL compute shaders through
+ * core::Sort (src/core/Sort.h:20-39) and util::runProg (src/core/util.cpp:32-36). Every entry
+ * point below names the reference member it replaces. All entry points are plain C: POD structs,
+ * plain pointers and sizes, a status code, and a thread-local error message.
+ *
+ * Buffers (all device memory is owned by the library; see wc_device_buffers):
+ *   state buffer   = the reference's particle_buffer1_ (Fluid.h:135): particles after update(),
+ *                    stored in the order of the last sort, exactly as the reference leaves them.
+ *   sorted buffer  = particle_buffer2_ (Fluid.h:136): Sort::run's output, density written in place.
+ *   cell tables    = Sort's count_buffer_/offset_buffer_ (Sort.h:70), sized by the cell count.
+ * The library stores particles as SoA float4 pairs (position+density, velocity+pressure), which
+ * holds the same 32 bytes per particle as the reference's AoS `struct Particle` (util.h:29-35).
+ * wc_particle is that AoS struct, used for host copies.
+ *
+ * Threading: a wc_fluid is not thread-safe. All work is enqueued on the handle's own CUDA stream;
+ * wc_fluid_update returns without waiting, and every copy-to-host call synchronises that stream.
+ */
+#ifndef WATERCUBE_H
+#define WATERCUBE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define WC_API __attribute__((visibility("default")))
+#else
+#define WC_API
+#endif
+
+#define WC_API_VERSION 1
+
+/* Status codes. The reference has none (it asserts, src/core/Fluid.cpp:222-223). */
+typedef enum wc_status {
+    WC_OK = 0,
+    WC_ERR_INVALID_ARG = 1, /* bad parameter, size or pointer */
+    WC_ERR_OOM = 2,         /* device or pinned host allocation failed */
+    WC_ERR_CUDA = 3,        /* a CUDA runtime call failed (no device, launch error, ...) */
+    WC_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (prefix-scan look-back) */
+    WC_ERR_NUMERIC = 5,     /* a non-finite particle position was binned */
+    WC_ERR_STATE = 6,       /* call out of order (e.g. update before setup) */
+    WC_ERR_UNSUPPORTED = 7  /* feature not compiled in */
+} wc_status;
+
+/* Equation of state. */
+enum {
+    /* p = p0 + k((rho/rho0)^3 - 1): Desbrun & Cani form, the one the reference runs
+       (assets/fluid/density.comp:130-133). */
+    WC_EOS_DESBRUN_CUBIC = 0,
+    /* p = p0 + k(rho - rho0): the reference's commented-out Harada form (density.comp:129). */
+    WC_EOS_LINEAR = 1
+};
+
+/* Behaviour switches. The reference runs with the first four on. */
+enum {
+    WC_FLAG_WALL_DENSITY = 1u << 0, /* pseudo wall density, x4 (density.comp:57-79, incl. its z branch testing y) */
+    WC_FLAG_WALL_FORCE = 1u << 1,   /* spiky wall push, x0.01 (update.comp:71-100) */
+    WC_FLAG_SPEED_CLAMP = 1u << 2,  /* per-component velocity clamp to +-max_speed (update.comp:5,199) */
+    WC_FLAG_MOUSE_FORCE = 1u << 3,  /* repulsion from the mouse ray (update.comp:116-132) */
+    WC_FLAG_TRACK_IDS = 1u << 4,    /* carry each particle's original index through every sort */
+    WC_FLAG_NEIGHBOR_COUNTS = 1u << 5 /* write per-particle neighbour counts in the density pass */
+};
+
+/* The reference's four active behaviours. */
+#define WC_FLAGS_REFERENCE (WC_FLAG_WALL_DENSITY | WC_FLAG_WALL_FORCE | WC_FLAG_SPEED_CLAMP | WC_FLAG_MOUSE_FORCE)
+
+/*
+ * Simulation parameters: the reference's fluent setters (Fluid.h:37-48) and the constants
+ * Fluid::setup derives (Fluid.cpp:203-216). Fill with a preset, change fields, then
+ * wc_params_finalize derives the zero fields.
+ */
+typedef struct wc_params {
+    uint32_t num_particles; /* Fluid::numParticles */
+    uint32_t grid_res;      /* Fluid::gridRes: cells per axis. 0 -> floor(size / kernel_radius) */
+    float size;             /* Fluid::size: the domain is [0,size]^3 */
+    float particle_radius;  /* Fluid::particleRadius */
+    float kernel_radius;    /* h. 0 -> 4 * particle_radius (Fluid.cpp:209) */
+    float particle_mass;    /* m. 0 -> 8 * particle_radius (Fluid.cpp:210) */
+    float rest_density;     /* Fluid::restDensity */
+    float rest_pressure;    /* Fluid::restPressure */
+    float stiffness;        /* Fluid::stiffness */
+    float viscosity;        /* Fluid::viscosityCoefficient */
+    float gravity[3];       /* gravity_direction_ * gravity_strength_ (Fluid.cpp:310) */
+    float time_scale;       /* wc_fluid_update(time) integrates dt = float(time) * time_scale (Fluid.cpp:308) */
+    uint32_t eos;           /* WC_EOS_* */
+    uint32_t flags;         /* WC_FLAG_* */
+    float max_speed;        /* speed clamp, 50 in the reference (update.comp:5) */
+    float wall_damping;     /* velocity factor on wall contact: v *= -wall_damping (update.comp:202) */
+    float wall_border;      /* wall clamp distance (update.comp:203) */
+    float mouse_origin[3];  /* mouse ray, in the fluid's frame (Fluid::getRelativeMouseRay) */
+    float mouse_dir[3];
+    /* Derived by wc_params_finalize when zero: */
+    float bin_size;    /* size / grid_res (Fluid.cpp:208) */
+    float poly6_const; /* 315 / (64 pi h^9), computed in double, cast to float (Fluid.cpp:214) */
+    float spiky_const; /* -45 / (pi h^6) (Fluid.cpp:215) */
+    float visc_const;  /* 45 / (pi h^6) (Fluid.cpp:216) */
+    uint32_t reserved[4];
+} wc_params;
+
+/* AoS particle, bit-compatible with the reference's std430 `struct Particle` (util.h:29-35). */
+typedef struct wc_particle {
+    float position[3];
+    float density;
+    float velocity[3];
+    float pressure;
+} wc_particle;
+
+/* Which particle buffer a host copy reads or writes. */
+enum {
+    WC_BUFFER_STATE = 1, /* particle_buffer1_: the state update() leaves behind */
+    WC_BUFFER_SORTED = 2 /* particle_buffer2_: the sort's output (density/pressure after the density pass) */
+};
+
+/* Integer buffers a host copy can read (util::getUints, src/core/util.cpp:62-72). */
+enum {
+    WC_UINTS_CELL_KEYS = 1,      /* per input particle: its cell key (count.comp:31-33) */
+    WC_UINTS_PERMUTATION = 2,    /* per sorted slot: input index it came from (sort.comp:44) */
+    WC_UINTS_CELL_COUNTS = 3,    /* per cell: particle count (Sort::getCountBuffer) */
+    WC_UINTS_CELL_OFFSETS = 4,   /* per cell: exclusive prefix of counts (Sort::getOffsetBuffer) */
+    WC_UINTS_NEIGHBOR_COUNTS = 5,/* per sorted particle: neighbours j != i with |r| < h (needs WC_FLAG_NEIGHBOR_COUNTS) */
+    WC_UINTS_PARTICLE_IDS = 6    /* per state-buffer particle: original index (needs WC_FLAG_TRACK_IDS) */
+};
+
+/* Raw device pointers, borrowed: valid until the next wc_fluid_* call that runs a step, or destroy. */
+typedef struct wc_device_buffers {
+    void* state_pos_density;    /* float4[n]: x, y, z, density     (state buffer) */
+    void* state_vel_pressure;   /* float4[n]: vx, vy, vz, pressure (state buffer) */
+    void* sorted_pos_density;   /* float4[n]  (sorted buffer) */
+    void* sorted_vel_pressure;  /* float4[n]  (sorted buffer) */
+    void* cell_keys;            /* uint32[n] */
+    void* permutation;          /* uint32[n] */
+    void* cell_start;           /* uint32[num_cells + 1]: cell c holds sorted slots [start[c], start[c+1]) */
+    void* neighbor_counts;      /* uint32[n] or NULL */
+    void* particle_ids;         /* uint32[n] or NULL */
+    void* stream;               /* cudaStream_t the handle enqueues on */
+    uint32_t num_particles;
+    uint32_t num_cells;
+} wc_device_buffers;
+
+typedef struct wc_fluid wc_fluid;
+
+/* ---- parameters ---------------------------------------------------------------------------- */
+
+/* The reference's constructor defaults (src/core/Fluid.cpp:9-27): 80,000 particles, gridRes 21,
+   r = 0.01, rho0 = 500, mu = 200, k = 100, p0 = 0, g = 900 down, time scale 0.012, cubic EOS,
+   WC_FLAGS_REFERENCE, a mouse ray that misses the box. */
+WC_API void wc_params_reference_defaults(wc_params* p);
+
+/* Dam-break preset: unit box, h = 0.0457 * (16384/n)^(1/3), lattice spacing h/2,
+   m = 1000 (h/2)^3, rho0 = 1000, k = 3, mu = 3.5, g = (0,-9.81,0), linear EOS, restitution 0.5,
+   no reference-only extras, grid_res = floor(1/h). n = 16384 and n = 1048576 are the two sizes
+   this solver is benchmarked at. */
+WC_API void wc_params_dam_break(wc_params* p, uint32_t num_particles);
+
+/* Fill derived fields and validate. WC_ERR_INVALID_ARG when the grid cannot hold the kernel
+   (bin_size < kernel_radius) or a value is out of range. */
+WC_API wc_status wc_params_finalize(wc_params* p);
+
+/* Largest float x with sqrtf(x) < h: |r| < h  <=>  dot(r,r) <= this (exact for IEEE sqrt). */
+WC_API float wc_cull_threshold(float kernel_radius);
+
+/* ---- initial states (host only) ---------------------------------------------------------- */
+
+/* The reference's dam-break lattice (Fluid::generateInitialParticles, Fluid.cpp:104-134):
+   ceil(cbrt(n)) per side, spacing 1.75 r, jitter in [-0.25, 0.25) * spacing per component.
+   MSVC rand() is replaced by splitmix64(seed). */
+WC_API wc_status wc_generate_reference_lattice(const wc_params* p, uint64_t seed, wc_particle* out, uint32_t n);
+
+/* The dam-break preset's block: spacing s = h/2, nx = nz = floor(cbrt(n/2)), ny = ceil(n/(nx nz)),
+   site (i,j,k) at ((i+.5)s, (j+.5)s, (k+.5)s) filled x fastest, then z, then y; first n sites;
+   each component jittered by (2u-1) * 0.01 h with u = top 24 bits of splitmix64(seed) * 2^-24,
+   three draws per particle in x, y, z order. */
+WC_API wc_status wc_generate_dam_break(const wc_params* p, uint64_t seed, wc_particle* out, uint32_t n);
+
+/* ---- the fluid (core::Fluid) ------------------------------------------------------------- */
+
+/* Fluid::create + the fluent setters: copies params (finalizing them) and allocates every device
+   buffer. Fails with WC_ERR_CUDA when no CUDA device is present. */
+WC_API wc_status wc_fluid_create(const wc_params* p, wc_fluid** out);
+
+/* Fluid::setup's buffer upload (Fluid.cpp:139-166): copy n == num_particles initial particles
+   into the state buffer. Must be called once before the first step; may be called again to reset. */
+WC_API wc_status wc_fluid_setup(wc_fluid* f, const wc_particle* initial, uint32_t n);
+
+/* Fluid::update(double time) (Fluid.cpp:342-354): sort, density, forces+integration with
+   dt = float(time) * time_scale. Asynchronous on the handle's stream (CUDA-graph launched). */
+WC_API wc_status wc_fluid_update(wc_fluid* f, double time);
+
+/* nsteps updates with dt given directly (time_scale not applied). */
+WC_API wc_status wc_fluid_step(wc_fluid* f, float dt, uint32_t nsteps);
+
+/* The three stages of one update, for inspection: Sort::run (Sort.cpp:254-267),
+   Fluid::runDensityProg (Fluid.cpp:268-289), Fluid::runUpdateProg (Fluid.cpp:294-321). */
+WC_API wc_status wc_fluid_sort(wc_fluid* f);
+WC_API wc_status wc_fluid_density(wc_fluid* f);
+WC_API wc_status wc_fluid_integrate(wc_fluid* f, float dt);
+
+/* Fluid::setMouseRay (Fluid.h:52) in the fluid's own frame. */
+WC_API wc_status wc_fluid_set_mouse_ray(wc_fluid* f, const float origin[3], const float dir[3]);
+/* gravity_direction_ * gravity_strength_ (Fluid::updateGravity / gravityStrength). */
+WC_API wc_status wc_fluid_set_gravity(wc_fluid* f, const float gravity[3]);
+
+/* util::getParticles (util.cpp:42-60): synchronise and copy n particles of a buffer to host. */
+WC_API wc_status wc_fluid_get_particles(wc_fluid* f, int buffer, wc_particle* out, uint32_t n);
+/* util::setParticles (util.cpp:74-78): overwrite a buffer from host. */
+WC_API wc_status wc_fluid_set_particles(wc_fluid* f, int buffer, const wc_particle* in, uint32_t n);
+/* util::getUints (util.cpp:62-72): synchronise and copy an integer buffer (WC_UINTS_*). n must
+   equal its length: num_particles, or num_cells for the two cell tables. */
+WC_API wc_status wc_fluid_get_uints(wc_fluid* f, int which, uint32_t* out, size_t n);
+
+WC_API wc_status wc_fluid_get_params(const wc_fluid* f, wc_params* out);
+WC_API wc_status wc_fluid_get_device_buffers(wc_fluid* f, wc_device_buffers* out);
+
+/* Wait for the handle's stream and report any device-side error flag raised since the last call
+   (WC_ERR_NUMERIC, WC_ERR_TIMEOUT). */
+WC_API wc_status wc_fluid_synchronize(wc_fluid* f);
+
+/* Steps taken since setup. */
+WC_API uint64_t wc_fluid_step_count(const wc_fluid* f);
+
+WC_API void wc_fluid_destroy(wc_fluid* f);
+
+/* ---- timing (CUDA events on the handle's stream) ---------------------------------------- */
+
+/* Number of kernels one step launches, and their names (index 0 .. count-1). */
+WC_API uint32_t wc_step_kernel_count(void);
+WC_API const char* wc_step_kernel_name(uint32_t index);
+
+/*
+ * Run nsteps steps of dt, each preceded (outside its timed span) by an L2 flush when flush_l2 is
+ * non-zero. step_ms[s] receives the device time of step s (graph launch, CUDA events).
+ * kernel_ms, when not NULL, receives nsteps * wc_step_kernel_count() per-kernel times from a
+ * second, separately launched run of the same steps with an event between kernels.
+ */
+WC_API wc_status wc_fluid_time_steps(wc_fluid* f, float dt, uint32_t nsteps, int flush_l2, float* step_ms,
+                                     float* kernel_ms);
+
+/* Make `device` current for handles created afterwards on this thread (one process per GPU). */
+WC_API wc_status wc_set_device(int device);
+WC_API int wc_device_count(void);
+
+/* Page-locked host memory for the host copies (faster and asynchronous-capable transfers). */
+WC_API wc_status wc_alloc_host(size_t bytes, void** out);
+WC_API void wc_free_host(void* p);
+
+/* ---- errors and build info -------------------------------------------------------------- */
+
+/* Message of the last failing call on this thread ("" if none). */
+WC_API const char* wc_last_error(void);
+WC_API const char* wc_status_string(wc_status s);
+/* e.g. "watercube 1 sm_103a" */
+WC_API const char* wc_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WATERCUBE_H */

@@ -1,0 +1,86 @@
+"""The core::Fluid-shaped API on the GPU: update(time) semantics, stage-by-stage calls equal
+the graph-launched step, host copies, device buffers, timing."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import case, fluid
+from watercube_gb300 import _abi
+from watercube_gb300.fluid import Fluid
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_usage_pattern(gpu):
+    """Fluid::create -> setters -> setup -> update(frame seconds), as WaterCubeApp drives it."""
+    f = Fluid.create("fluid").numParticles(20000).gridRes(21).viscosityCoefficient(200).stiffness(100)
+    f.setup()
+    for _ in range(3):
+        f.update(1.0 / 60.0)
+    out = f.particles()
+    f.synchronize()
+    assert out.shape == (20000,) and np.isfinite(out["position"]).all()
+    assert f.step_count == 3
+    f.close()
+
+
+def test_update_time_scale_equals_step(gpu):
+    p, st = case("refdefaults")
+    with fluid(p, st) as a, fluid(p, st) as b:
+        a.update(1.0 / 60.0)
+        b.step(np.float32(1.0 / 60.0) * np.float32(0.012), 1)
+        assert a.particles().tobytes() == b.particles().tobytes()
+
+
+def test_stages_equal_graph_step(gpu):
+    p, st = case("dam16k")
+    dts = [1e-3, 5e-4, 1e-3]
+    with fluid(p, st) as a, fluid(p, st) as b:
+        for dt in dts:
+            a.step(dt, 1)  # graph, re-parameterised when dt changes
+            b.sort()
+            b.density()
+            b.integrate(dt)
+        assert a.particles().tobytes() == b.particles().tobytes()
+
+
+def test_host_copies_round_trip(gpu):
+    p, st = case("dam16k")
+    with fluid(p, st) as f:
+        assert f.particles().tobytes() == st.tobytes()
+        st2 = st.copy()
+        st2["velocity"] = 0.25
+        f.set_particles(st2, _abi.WC_BUFFER_SORTED)
+        assert f.particles(_abi.WC_BUFFER_SORTED).tobytes() == st2.tobytes()
+
+
+def test_device_buffers(gpu):
+    p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS | _abi.WC_FLAG_NEIGHBOR_COUNTS)
+    with fluid(p, st) as f:
+        b = f.device_buffers()
+        assert b.num_particles == st.shape[0] and b.num_cells == p.grid_res**3
+        for name in ("state_pos_density", "state_vel_pressure", "sorted_pos_density", "cell_start", "permutation",
+                     "neighbor_counts", "particle_ids", "stream"):
+            assert getattr(b, name)
+        assert b.state_pos_density % 16 == 0
+
+
+def test_gravity_and_mouse_setters(gpu):
+    p, st = case("dam16k")
+    with fluid(p, st) as a, fluid(p, st) as b:
+        b.setGravity([0.0, 0.0, 0.0])
+        a.step(1e-3, 2)
+        b.step(1e-3, 2)
+        va, vb = a.particles()["velocity"], b.particles()["velocity"]
+        assert va[:, 1].mean() < vb[:, 1].mean()
+
+
+def test_timing_entry_point(gpu):
+    p, st = case("dam16k")
+    with fluid(p, st) as f:
+        ms, kern = f.time_steps(1e-3, 4, flush_l2=True, kernel_times=True)
+        assert (ms > 0).all() and kern.shape == (4, 6) and (kern >= 0).all()
+        assert Fluid.kernel_names() == ["bin_count", "scan_cells", "scatter_cells", "rank_gather", "density",
+                                        "force_integrate"]
+        assert f.step_count == 8

@@ -1,0 +1,127 @@
+"""Edge cases on the GPU: empty and single-particle fluids, coincident particles, a particle
+at p = size, all particles in one cell, non-finite input (reported, not faulted)."""
+import numpy as np
+import pytest
+
+from helpers import case, fluid
+from oracle.oracle import to64
+from watercube_gb300 import _abi
+from watercube_gb300.fluid import Fluid, dam_break_params, finalize
+
+pytestmark = pytest.mark.gpu
+
+
+def small(n, flags=_abi.WC_FLAG_NEIGHBOR_COUNTS):
+    p = dam_break_params(16384)
+    p.num_particles = n
+    p.flags |= flags
+    return finalize(p)
+
+
+def states(positions):
+    s = np.zeros(len(positions), _abi.PARTICLE_DTYPE)
+    if len(positions):
+        s["position"] = np.asarray(positions, np.float32)
+    return s
+
+
+def test_empty_fluid(gpu):
+    p = small(0)
+    with fluid(p, states([])) as f:
+        f.step(1e-3, 3)
+        f.synchronize()
+        assert f.particles().shape == (0,)
+        assert f.cell_counts().sum() == 0
+
+
+def test_single_particle_free_fall(gpu, oracle):
+    p = small(1)
+    st = states([[0.5, 0.5, 0.5]])
+    with fluid(p, st) as f:
+        f.step(1e-3, 10)
+        out = f.particles()
+    ref = to64(st)
+    oracle.step(p, ref, 1e-3, 10)
+    assert np.allclose(out["position"], ref["position"], rtol=0, atol=1e-6)
+    assert np.allclose(out["velocity"], ref["velocity"], rtol=1e-5)
+
+
+def test_coincident_particles(gpu, oracle):
+    p = small(3)
+    st = states([[0.4, 0.4, 0.4], [0.4, 0.4, 0.4], [0.41, 0.4, 0.4]])
+    with fluid(p, st) as f:
+        f.sort()
+        f.density()
+        srt = f.particles(_abi.WC_BUFFER_SORTED)
+        nc = f.neighbor_counts()
+        f.integrate(1e-3)
+        out = f.particles()
+    assert list(nc) == [2, 2, 2]
+    assert np.isfinite(out["position"]).all() and np.isfinite(out["velocity"]).all()
+    s64, _, _, counts, offsets = oracle.sort(p, to64(st))
+    oracle.density(p, s64, counts, offsets)
+    assert np.allclose(srt["density"], s64["density"], rtol=1e-5)
+
+
+def test_particle_at_box_faces(gpu, oracle):
+    p = small(4)
+    st = states([[1.0, 1.0, 1.0], [0.0, 0.0, 0.0], [1.0, 0.5, 0.0], [0.999, 0.999, 0.999]])
+    with fluid(p, st) as f:
+        f.step(1e-3, 1)
+        out = f.particles()
+        keys = f.keys()
+    assert np.isfinite(out["position"]).all()
+    border = np.float32(p.wall_border)
+    assert (out["position"] >= border).all() and (out["position"] <= np.float32(1.0) - border).all()
+    _, okeys, _, _, _ = oracle.sort(p, out)
+    assert keys.shape == okeys.shape
+
+
+def test_all_in_one_cell_density(gpu, oracle):
+    p, st = case("dam16k", _abi.WC_FLAG_NEIGHBOR_COUNTS)
+    n = 2000
+    p = p.copy()
+    p.num_particles = n
+    rng = np.random.default_rng(2)
+    b = float(p.bin_size)
+    st = states(0.5 + rng.uniform(0.1 * b, 0.9 * b, size=(n, 3)))
+    with fluid(p, st) as f:
+        f.sort()
+        f.density()
+        srt = f.particles(_abi.WC_BUFFER_SORTED)
+        nc = f.neighbor_counts()
+    o_sorted, _, _, counts, offsets = oracle.sort(p, st)
+    nc32 = oracle.density(p, o_sorted, counts, offsets)
+    assert np.array_equal(nc, nc32)
+    s64 = to64(srt)
+    oracle.density(p, s64, counts, offsets)
+    assert (np.abs(srt["density"] - s64["density"]) / np.abs(s64["density"])).max() <= 1e-5
+
+
+def test_nonfinite_position_is_reported(gpu):
+    p = small(64)
+    rng = np.random.default_rng(3)
+    st = states(rng.uniform(0.3, 0.6, size=(64, 3)))
+    st["position"][5, 1] = np.nan
+    with fluid(p, st) as f:
+        f.step(1e-3, 1)
+        with pytest.raises(_abi.WatercubeError) as e:
+            f.synchronize()
+        assert e.value.status == _abi.WC_ERR_NUMERIC
+        # the error is reported once and cleared; the handle stays usable
+        good = states(rng.uniform(0.3, 0.6, size=(64, 3)))
+        f.set_particles(good)
+        f.step(1e-3, 1)
+        f.synchronize()
+
+
+def test_wrong_sizes_rejected(gpu):
+    p = small(10)
+    with fluid(p, states(np.full((10, 3), 0.5))) as f:
+        with pytest.raises(_abi.WatercubeError) as e:
+            f.set_particles(states(np.full((11, 3), 0.5)))
+        assert e.value.status == _abi.WC_ERR_INVALID_ARG
+    f = Fluid.create("x", p)
+    with pytest.raises(_abi.WatercubeError):
+        f.setup(states(np.full((9, 3), 0.5)))
+    f.close()

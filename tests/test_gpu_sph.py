@@ -1,0 +1,130 @@
+"""Density, pressure, forces and integration on the GPU against the oracle.
+
+  * per-particle neighbour counts: bit-exact against the reference stage logic (FP32 oracle);
+  * density: max relative error <= 1e-5 against the FP64 oracle on the same input state;
+  * pressure: the same bound propagated through the equation of state;
+  * one force + integration pass: velocity error <= 1e-4 of the largest velocity change, on
+    the same input state, against the FP64 oracle;
+  * 200 steps of the 16,384-particle dam break: position drift against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from helpers import case, evolved, fluid
+from oracle.oracle import to64
+from watercube_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+
+DENSITY_RTOL = 1e-5
+
+CASES = [
+    ("dam16k", 30, 1e-3),
+    ("refdefaults", 20, 2e-4),
+    ("dam16k_refphysics", 10, 2e-4),
+    ("dam1m", 4, 2.5e-4),
+]
+
+
+def gpu_density(p, st):
+    with fluid(p, st) as f:
+        f.sort()
+        f.density()
+        return f.particles(_abi.WC_BUFFER_SORTED), f.neighbor_counts(), f.permutation()
+
+
+def eos_tolerance(p, rho64):
+    k = float(p.stiffness)
+    if p.eos == _abi.WC_EOS_LINEAR:
+        return DENSITY_RTOL * k * np.abs(rho64) + 1e-6
+    x = rho64 / float(p.rest_density)
+    return DENSITY_RTOL * 3.0 * k * np.abs(x) ** 3 + 1e-6
+
+
+@pytest.mark.parametrize("name,steps,dt", CASES)
+def test_density_pressure_neighbours(gpu, oracle, name, steps, dt):
+    p, st = evolved(name, steps, dt, _abi.WC_FLAG_NEIGHBOR_COUNTS)
+    srt, nc, perm = gpu_density(p, st)
+    o_sorted, _, o_perm, counts, offsets = oracle.sort(p, st)
+    assert np.array_equal(perm, o_perm)
+    nc32 = oracle.density(p, o_sorted, counts, offsets)
+    assert np.array_equal(nc, nc32), f"neighbour counts differ at {np.flatnonzero(nc != nc32)[:10]}"
+    s64 = to64(srt)
+    oracle.density(p, s64, counts, offsets)
+    rel = np.abs(srt["density"] - s64["density"]) / np.abs(s64["density"])
+    assert rel.max() <= DENSITY_RTOL, f"max rel density err {rel.max():.3e}"
+    # pressure uses the density without the wall term; compare through the EOS bound
+    if p.flags & _abi.WC_FLAG_WALL_DENSITY:
+        no_wall = p.copy()
+        no_wall.flags &= ~_abi.WC_FLAG_WALL_DENSITY
+        t64 = to64(srt)
+        oracle.density(no_wall, t64, counts, offsets)
+        rho_nw = t64["density"]
+    else:
+        rho_nw = s64["density"]
+    perr = np.abs(srt["pressure"] - s64["pressure"])
+    assert (perr <= eos_tolerance(p, rho_nw)).all(), f"max pressure err {perr.max():.3e}"
+
+
+@pytest.mark.parametrize("name,steps,dt", CASES)
+def test_force_integration_pass(gpu, oracle, name, steps, dt):
+    p, st = evolved(name, steps, dt)
+    with fluid(p, st) as f:
+        f.sort()
+        f.density()
+        srt = f.particles(_abi.WC_BUFFER_SORTED)
+        f.integrate(dt)
+        out = f.particles(_abi.WC_BUFFER_STATE)
+    _, _, _, counts, offsets = oracle.sort(p, st)
+    s64 = to64(srt)
+    o64 = oracle.update(p, s64, counts, offsets, dt)
+    dv = np.abs(o64["velocity"] - s64["velocity"]).max()
+    verr = np.abs(out["velocity"] - o64["velocity"]).max()
+    assert verr <= 1e-4 * dv + 1e-7, f"velocity err {verr:.3e} vs max change {dv:.3e}"
+    perr = np.abs(out["position"] - o64["position"]).max()
+    assert perr <= 1e-4 * dv * dt + 1e-6 * float(p.kernel_radius), f"position err {perr:.3e}"
+    # density and pressure are carried through the update unchanged
+    assert np.array_equal(out["density"], srt["density"])
+    assert np.array_equal(out["pressure"], srt["pressure"])
+
+
+def test_position_drift_200_steps(gpu, oracle):
+    """The 16,384-particle dam break for 200 steps of 1 ms against the FP64 oracle."""
+    p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
+    h = float(p.kernel_radius)
+    with fluid(p, st) as f:
+        f.step(1e-3, 200)
+        out = f.particles()
+        ids = f.particle_ids()
+    assert np.array_equal(np.sort(ids), np.arange(st.shape[0], dtype=np.uint32))
+    s64 = to64(st)
+    ids64 = np.arange(st.shape[0], dtype=np.uint32)
+    oracle.step(p, s64, 1e-3, 200, ids64)
+    pg = np.empty((st.shape[0], 3))
+    po = np.empty((st.shape[0], 3))
+    pg[ids] = out["position"]
+    po[ids64] = s64["position"]
+    drift = np.abs(pg - po).max()
+    print(f"200-step drift: {drift:.3e} = {drift / h:.3e} h")
+    assert drift <= 1e-4 * h, f"drift {drift / h:.3e} h"
+
+
+def test_reference_physics_tracks_oracle(gpu, oracle):
+    """The reference's own physics (cubic EOS, wall terms, clamp) over several full steps."""
+    p, st = case("refdefaults", _abi.WC_FLAG_TRACK_IDS)
+    dt = 0.012 / 60.0
+    with fluid(p, st) as f:
+        for _ in range(5):
+            f.update(1.0 / 60.0)  # dt = time * time_scale, as Fluid::update
+        out = f.particles()
+        ids = f.particle_ids()
+    ref = st.copy()
+    ids32 = np.arange(st.shape[0], dtype=np.uint32)
+    oracle.step(p, ref, np.float32(1.0 / 60.0) * np.float32(0.012), 5, ids32)
+    pg = np.empty((st.shape[0], 3))
+    po = np.empty((st.shape[0], 3))
+    pg[ids] = out["position"]
+    po[ids32] = ref["position"]
+    err = np.abs(pg - po).max()
+    assert err <= 1e-5 * float(p.kernel_radius), f"{err:.3e}"
+    assert dt > 0

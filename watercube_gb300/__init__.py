@@ -1,0 +1,12 @@
+"""GB300 SPH water solver: the WaterCube simulation path (core::Fluid + core::Sort and their
+compute shaders) as hand-written sm_103a CUDA behind a C ABI (include/watercube.h)."""
+from ._abi import PARTICLE_DTYPE, Params, WatercubeError  # noqa: F401
+from .fluid import (  # noqa: F401
+    Fluid,
+    PinnedBuffer,
+    dam_break_params,
+    finalize,
+    generate_dam_break,
+    generate_reference_lattice,
+    reference_params,
+)

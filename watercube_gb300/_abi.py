@@ -1,0 +1,195 @@
+"""ctypes view of include/watercube.h and the loader of libwatercube.so.
+
+The library is the product; this module only declares its C ABI for Python callers. Loading
+fails loudly (WatercubeError) when the shared library has not been built: there is no
+fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libwatercube.so"
+
+# wc_status
+WC_OK = 0
+WC_ERR_INVALID_ARG = 1
+WC_ERR_OOM = 2
+WC_ERR_CUDA = 3
+WC_ERR_TIMEOUT = 4
+WC_ERR_NUMERIC = 5
+WC_ERR_STATE = 6
+WC_ERR_UNSUPPORTED = 7
+
+WC_EOS_DESBRUN_CUBIC = 0
+WC_EOS_LINEAR = 1
+
+WC_FLAG_WALL_DENSITY = 1 << 0
+WC_FLAG_WALL_FORCE = 1 << 1
+WC_FLAG_SPEED_CLAMP = 1 << 2
+WC_FLAG_MOUSE_FORCE = 1 << 3
+WC_FLAG_TRACK_IDS = 1 << 4
+WC_FLAG_NEIGHBOR_COUNTS = 1 << 5
+WC_FLAGS_REFERENCE = WC_FLAG_WALL_DENSITY | WC_FLAG_WALL_FORCE | WC_FLAG_SPEED_CLAMP | WC_FLAG_MOUSE_FORCE
+
+WC_BUFFER_STATE = 1
+WC_BUFFER_SORTED = 2
+
+WC_UINTS_CELL_KEYS = 1
+WC_UINTS_PERMUTATION = 2
+WC_UINTS_CELL_COUNTS = 3
+WC_UINTS_CELL_OFFSETS = 4
+WC_UINTS_NEIGHBOR_COUNTS = 5
+WC_UINTS_PARTICLE_IDS = 6
+
+
+class WatercubeError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("num_particles", C.c_uint32),
+        ("grid_res", C.c_uint32),
+        ("size", C.c_float),
+        ("particle_radius", C.c_float),
+        ("kernel_radius", C.c_float),
+        ("particle_mass", C.c_float),
+        ("rest_density", C.c_float),
+        ("rest_pressure", C.c_float),
+        ("stiffness", C.c_float),
+        ("viscosity", C.c_float),
+        ("gravity", C.c_float * 3),
+        ("time_scale", C.c_float),
+        ("eos", C.c_uint32),
+        ("flags", C.c_uint32),
+        ("max_speed", C.c_float),
+        ("wall_damping", C.c_float),
+        ("wall_border", C.c_float),
+        ("mouse_origin", C.c_float * 3),
+        ("mouse_dir", C.c_float * 3),
+        ("bin_size", C.c_float),
+        ("poly6_const", C.c_float),
+        ("spiky_const", C.c_float),
+        ("visc_const", C.c_float),
+        ("reserved", C.c_uint32 * 4),
+    ]
+
+    def copy(self) -> "Params":
+        p = Params()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(Params))
+        return p
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+class DeviceBuffers(C.Structure):
+    _fields_ = [
+        ("state_pos_density", C.c_void_p),
+        ("state_vel_pressure", C.c_void_p),
+        ("sorted_pos_density", C.c_void_p),
+        ("sorted_vel_pressure", C.c_void_p),
+        ("cell_keys", C.c_void_p),
+        ("permutation", C.c_void_p),
+        ("cell_start", C.c_void_p),
+        ("neighbor_counts", C.c_void_p),
+        ("particle_ids", C.c_void_p),
+        ("stream", C.c_void_p),
+        ("num_particles", C.c_uint32),
+        ("num_cells", C.c_uint32),
+    ]
+
+
+# numpy view of `struct wc_particle` (the reference's std430 Particle, 32 bytes)
+PARTICLE_DTYPE = np.dtype(
+    [("position", np.float32, (3,)), ("density", np.float32), ("velocity", np.float32, (3,)), ("pressure", np.float32)]
+)
+assert PARTICLE_DTYPE.itemsize == 32
+
+_lib = None
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _declare(lib) -> None:
+    S = C.c_int
+    P = C.c_void_p
+    pp = C.POINTER(Params)
+    sig = {
+        "wc_params_reference_defaults": (None, [pp]),
+        "wc_params_dam_break": (None, [pp, C.c_uint32]),
+        "wc_params_finalize": (S, [pp]),
+        "wc_cull_threshold": (C.c_float, [C.c_float]),
+        "wc_generate_reference_lattice": (S, [pp, C.c_uint64, P, C.c_uint32]),
+        "wc_generate_dam_break": (S, [pp, C.c_uint64, P, C.c_uint32]),
+        "wc_fluid_create": (S, [pp, C.POINTER(P)]),
+        "wc_fluid_setup": (S, [P, P, C.c_uint32]),
+        "wc_fluid_update": (S, [P, C.c_double]),
+        "wc_fluid_step": (S, [P, C.c_float, C.c_uint32]),
+        "wc_fluid_sort": (S, [P]),
+        "wc_fluid_density": (S, [P]),
+        "wc_fluid_integrate": (S, [P, C.c_float]),
+        "wc_fluid_set_mouse_ray": (S, [P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "wc_fluid_set_gravity": (S, [P, C.POINTER(C.c_float)]),
+        "wc_fluid_get_particles": (S, [P, C.c_int, P, C.c_uint32]),
+        "wc_fluid_set_particles": (S, [P, C.c_int, P, C.c_uint32]),
+        "wc_fluid_get_uints": (S, [P, C.c_int, P, C.c_size_t]),
+        "wc_fluid_get_params": (S, [P, pp]),
+        "wc_fluid_get_device_buffers": (S, [P, C.POINTER(DeviceBuffers)]),
+        "wc_fluid_synchronize": (S, [P]),
+        "wc_fluid_step_count": (C.c_uint64, [P]),
+        "wc_fluid_destroy": (None, [P]),
+        "wc_step_kernel_count": (C.c_uint32, []),
+        "wc_step_kernel_name": (C.c_char_p, [C.c_uint32]),
+        "wc_fluid_time_steps": (S, [P, C.c_float, C.c_uint32, C.c_int, P, P]),
+        "wc_set_device": (S, [C.c_int]),
+        "wc_device_count": (C.c_int, []),
+        "wc_alloc_host": (S, [C.c_size_t, C.POINTER(P)]),
+        "wc_free_host": (None, [P]),
+        "wc_last_error": (C.c_char_p, []),
+        "wc_status_string": (C.c_char_p, [S]),
+        "wc_build_info": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib():
+    """The loaded libwatercube.so. Raises WatercubeError when it is missing."""
+    global _lib
+    if _lib is None:
+        path = Path(os.environ.get("WATERCUBE_LIB", LIB_PATH))
+        if not path.is_file():
+            raise WatercubeError(
+                WC_ERR_UNSUPPORTED,
+                f"{path} is not built; run `python -c 'import __graft_entry__ as g; g.build()'`",
+            )
+        handle = C.CDLL(str(path))
+        _declare(handle)
+        _lib = handle
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != WC_OK:
+        msg = lib().wc_last_error().decode() or lib().wc_status_string(status).decode()
+        raise WatercubeError(status, f"{what}: {msg}" if what else msg)
+
+
+def particles(n: int) -> np.ndarray:
+    return np.zeros(n, dtype=PARTICLE_DTYPE)

@@ -1,0 +1,96 @@
+// wc_internal.h — device-side constants, buffer sets and stage launchers shared by the
+// solver's translation units. Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/watercube.h"
+
+namespace wc {
+
+// Device error bits (OR-ed into DevBuffers::err by kernels; read at synchronisation points).
+enum : uint32_t {
+    DEVERR_NONFINITE = 1u << 0,    // a non-finite position was binned
+    DEVERR_SCAN_TIMEOUT = 1u << 1  // a scan tile gave up waiting on its predecessor
+};
+
+// Constants of one scene, by value in kernel parameters (single scene) or in a device table
+// (batched scenes).
+struct SceneConsts {
+    float size, bin, h, h2, cull;  // cull: largest d2 with sqrtf(d2) < h
+    float m, rho0, p0, k, mu;
+    float c6, cs, cv;
+    float max_speed, damping, border;
+    float g[3];
+    float mouse_o[3], mouse_d[3];
+    int32_t R;
+    uint32_t eos, flags;
+};
+
+// Per-step inputs that may change between steps without re-recording the step graph.
+struct StepInputs {
+    float dt;
+    float g[3];
+    float mouse_o[3], mouse_d[3];
+};
+
+// Decoupled look-back scan over the cell histogram.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;  // ~0.3-1 s of polling before giving up
+
+// Force kernel: per-lane neighbour list capacity (shared memory, [CAP][32] per warp).
+constexpr int FORCE_LIST_CAP = 48;
+constexpr int SPH_THREADS = 256;
+
+struct DevBuffers {
+    uint32_t n;          // particles
+    uint32_t num_cells;  // R^3
+    uint32_t num_tiles;  // scan tiles
+    // particle state: A = state buffer (particle_buffer1_), B = sorted buffer (particle_buffer2_)
+    float4 *pos_a, *vel_a, *pos_b, *vel_b;
+    uint32_t *ids_a, *ids_b;  // original indices (WC_FLAG_TRACK_IDS), else null
+    // sort
+    uint32_t *keys, *ranks, *unordered, *perm;
+    uint32_t *counts;     // [C] histogram (zero between steps)
+    uint32_t *start;      // [C+1] exclusive prefix + total
+    uint32_t *cell_list;  // [C] non-empty cells, ascending
+    uint32_t *num_nonempty;
+    unsigned long long* scan_desc;  // [num_tiles]
+    uint32_t* scan_tile_counter;
+    uint32_t* ncount;  // [n] or null
+    uint32_t* err;
+};
+
+// Launch geometry computed once per handle.
+struct LaunchDims {
+    int sms;
+    int grid_stream;   // blocks for the per-particle kernels
+    int grid_density;  // persistent blocks
+    int grid_force;
+};
+
+LaunchDims compute_launch_dims(int device);
+
+// Stage launchers (wc_sort.cu, wc_sph.cu). All enqueue on `s` and never synchronise.
+void launch_bin_count(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
+void launch_scan_cells(const DevBuffers& d, cudaStream_t s);
+void launch_scatter(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s);
+void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s);
+void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
+void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
+                  cudaStream_t s);
+// AoS <-> SoA for host copies through a contiguous staging buffer.
+void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, cudaStream_t s);
+void launch_soa_to_aos(const float4* pos, const float4* vel, float4* aos, uint32_t n, cudaStream_t s);
+void launch_l2_flush(const float4* buf, size_t n4, float* sink, cudaStream_t s);
+
+// The kernel entry points the force node of a captured graph is recognised by.
+const void* force_kernel_symbol(uint32_t flags);
+
+SceneConsts make_scene_consts(const wc_params& p);
+StepInputs make_step_inputs(const wc_params& p, float dt);
+
+}  // namespace wc

@@ -1,0 +1,22 @@
+// wc_util.h — error reporting helpers shared by the host translation units.
+#pragma once
+
+#include "../../include/watercube.h"
+
+namespace wc {
+
+// Record a message for wc_last_error() and return `s`.
+wc_status fail(wc_status s, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+void clear_error();
+const char* last_error();
+
+}  // namespace wc
+
+// Return WC_ERR_CUDA (with the call text and CUDA's message) when a runtime call fails.
+#define WC_CUDA_TRY(call)                                                                        \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return ::wc::fail(e_ == cudaErrorMemoryAllocation ? WC_ERR_OOM : WC_ERR_CUDA,        \
+                              "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
