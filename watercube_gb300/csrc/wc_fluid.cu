@@ -33,9 +33,11 @@ struct ForceArgs {
     const uint32_t* start;
     const uint32_t* cell_list;
     const uint32_t* num_nonempty;
-    void* ptrs[12];
+    const uint32_t* hits;
+    void* ptrs[13];
     void bind() {
-        void* p[12] = {&sc, &in, &n, &pos_b, &vel_b, &ids_b, &pos_a, &vel_a, &ids_a, &start, &cell_list, &num_nonempty};
+        void* p[13] = {&sc,    &in,    &n,     &pos_b, &vel_b,     &ids_b,        &pos_a,
+                       &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits};
         std::memcpy(ptrs, p, sizeof p);
     }
 };
@@ -91,7 +93,7 @@ void free_all(wc_fluid* f) {
     void* ptrs[] = {d.pos_a,     d.vel_a,        d.pos_b,     d.vel_b,    d.ids_a,           d.ids_b,
                     d.keys,      d.ranks,        d.unordered, d.perm,     d.counts,          d.start,
                     d.cell_list, d.num_nonempty, d.scan_desc, d.ncount,   d.scan_tile_counter, d.err,
-                    f->staging,  f->flush_buf,   f->flush_sink};
+                    d.hits,      f->staging,     f->flush_buf, f->flush_sink};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (f->h_err) cudaFreeHost(f->h_err);
@@ -120,6 +122,7 @@ wc_status allocate(wc_fluid* f) {
     WC_TRY(dalloc(&d.unordered, n));
     WC_TRY(dalloc(&d.perm, n));
     if (f->params.flags & WC_FLAG_NEIGHBOR_COUNTS) WC_TRY(dalloc(&d.ncount, n));
+    WC_TRY(dalloc(&d.hits, (size_t)n * MASK_WORDS));
     WC_TRY(dalloc(&d.counts, d.num_cells));
     WC_TRY(dalloc(&d.start, (size_t)d.num_cells + 1));
     WC_TRY(dalloc(&d.cell_list, d.num_cells));
@@ -140,6 +143,7 @@ wc_status allocate(wc_fluid* f) {
         WC_CUDA_TRY(cudaMemsetAsync(d.perm, 0, sizeof(uint32_t) * n, f->stream));
         WC_CUDA_TRY(cudaMemsetAsync(d.keys, 0, sizeof(uint32_t) * n, f->stream));
         if (d.ncount) WC_CUDA_TRY(cudaMemsetAsync(d.ncount, 0, sizeof(uint32_t) * n, f->stream));
+        WC_CUDA_TRY(cudaMemsetAsync(d.hits, 0, sizeof(uint32_t) * MASK_WORDS * (size_t)n, f->stream));
     }
     WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
     return WC_OK;
@@ -207,6 +211,7 @@ wc_status capture_graph(wc_fluid* f, const StepInputs& in) {
     a.start = f->d.start;
     a.cell_list = f->d.cell_list;
     a.num_nonempty = f->d.num_nonempty;
+    a.hits = f->d.hits;
     a.bind();
     f->graph_in = in;
     return WC_OK;

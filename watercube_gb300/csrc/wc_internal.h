@@ -41,9 +41,14 @@ constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;  // ~0.3-1 s of polling before giving up
 
-// Force kernel: per-lane neighbour list capacity (shared memory, [CAP][32] per warp).
-constexpr int FORCE_LIST_CAP = 48;
+// SPH passes: 256-thread blocks of 8 cell teams (one warp each).
 constexpr int SPH_THREADS = 256;
+// Candidates a warp stages in shared memory per cell (plus 64 padding entries).
+constexpr int STAGE_CAP = 320;
+// 32-bit words of neighbour bit strings per particle (density pass -> force pass).
+constexpr int MASK_WORDS = 16;
+// Force kernel direct path: per-lane neighbour list capacity ([CAP][32] words per warp).
+constexpr int FORCE_LIST_CAP = 24;
 
 struct DevBuffers {
     uint32_t n;          // particles
@@ -61,6 +66,7 @@ struct DevBuffers {
     unsigned long long* scan_desc;  // [num_tiles]
     uint32_t* scan_tile_counter;
     uint32_t* ncount;  // [n] or null
+    uint32_t* hits;    // [n * MASK_WORDS] neighbour bit strings
     uint32_t* err;
 };
 

@@ -9,15 +9,24 @@
 // Work decomposition (both kernels): a warp owns one non-empty cell at a time (grid-stride over
 // the cell list the scan produced). The 27 neighbour cells of a cell form 9 rows of 3 cells
 // that are contiguous in key order, hence 9 contiguous ranges of the sorted particle buffer;
-// lanes 0..8 look them up once per cell. The warp's 32 lanes are split into nt targets (the
-// cell's particles, up to 32 at a time) x S = floor(32/nt) slices; slice s of target t tests
-// candidates s, s+S, s+2S, ... of every row, so every lane of the warp runs the same trip count
-// and each candidate load is shared by the nt lanes that need it. Partial sums are combined
-// with shuffles in a fixed order: results are deterministic.
+// lanes 0..8 look them up once per cell and a 9-lane scan numbers the concatenated candidate
+// list 0 .. L-1. The warp's 32 lanes are split into nt targets (the cell's particles, up to 32
+// at a time) x S = floor(32/nt) slices; slice s of target t takes candidate pairs s, s+S, ...,
+// so every lane runs the same trip count. Partial sums are combined with shuffles in a fixed
+// order: results are deterministic.
+//
+// Density: the candidates' positions are staged in shared memory as x/y/z arrays and tested two
+// at a time with Blackwell's packed f32x2 FMA (one instruction updates both candidates). Each
+// lane records which of its candidates passed as a bit string (2 bits per pair); the force pass
+// replays exactly those bits instead of testing all candidates again. Cells whose candidate
+// list does not fit the stage, cells of more than 32 particles and bit strings longer than the
+// per-particle slot take the direct path: the density pass reads candidates from global memory
+// and the force pass culls into a per-lane shared-memory list.
 //
 // Neighbour test: |r| < h is evaluated exactly as sqrtf(fma(dz,dz,fma(dy,dy,dx*dx))) < h would
 // be, as d2 <= cull with cull = the largest float whose sqrtf is below h, so the neighbour
-// sets (and counts) are bit-identical to the reference stage logic's.
+// sets (and counts) are bit-identical to the reference stage logic's. The packed form computes
+// the same fused operations per element, so it agrees bit for bit.
 #include <cuda_runtime.h>
 
 #include "wc_internal.h"
@@ -26,16 +35,59 @@ namespace wc {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int WARPS = SPH_THREADS / 32;
+
+// ---- packed f32x2 arithmetic (two floats in one 64-bit register; lo = first) ---------------------
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float& a, float& b) { asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
 
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
-// Lanes 0..8 of the warp get the sorted-slot range [lo, hi) of neighbour row (dy, dz) of cell
-// (cx, cy, cz); other lanes (and rows outside the grid) get an empty range.
-__device__ __forceinline__ void row_range(const uint32_t* __restrict__ start, uint32_t n, int32_t R, int cx, int cy,
-                                          int cz, uint32_t lane, uint32_t& lo, uint32_t& hi) {
-    lo = hi = 0u;
+// ---- per-cell geometry ------------------------------------------------------------------------
+
+struct CellRows {
+    uint32_t cbeg, cend;    // the cell's own sorted slots
+    uint32_t lo, len, pex;  // lanes 0..8: row r's slot range and its offset in the concatenated list
+    uint32_t total;         // candidates in all 9 rows
+};
+
+// Row r = (dy, dz) = (r % 3 - 1, r / 3 - 1) of cell c: cells x-1..x+1 of that row, which are
+// consecutive keys, hence one slot range [start[first], start[last + 1]).
+__device__ __forceinline__ CellRows cell_rows(const uint32_t* __restrict__ start, uint32_t n, int32_t R, uint32_t c,
+                                              uint32_t lane) {
+    CellRows cr;
+    cr.cend = min(__ldg(start + c + 1), n);
+    cr.cbeg = min(__ldg(start + c), cr.cend);
+    const uint32_t uR = (uint32_t)R;
+    const int cx = (int)(c % uR), cy = (int)((c / uR) % uR), cz = (int)(c / (uR * uR));
+    uint32_t lo = 0, hi = 0;
     if (lane < 9u) {
         const int yy = cy + (int)(lane % 3u) - 1;
         const int zz = cz + (int)(lane / 3u) - 1;
@@ -51,6 +103,34 @@ __device__ __forceinline__ void row_range(const uint32_t* __restrict__ start, ui
             lo = min(lo, hi);
         }
     }
+    cr.lo = lo;
+    cr.len = hi - lo;
+    uint32_t x = cr.len;
+#pragma unroll
+    for (int off = 1; off < 16; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, x, off);
+        if ((int)lane >= off) x += y;
+    }
+    cr.pex = x - cr.len;
+    cr.total = __shfl_sync(FULL, x, 8);
+    return cr;
+}
+
+// Split the warp into nt targets x S slices: lane = t + sl * nt. floor() of (a + 0.5) / nt is
+// exact here: the fraction is at least 0.5/nt >= 1/64 from an integer and the float error is
+// below 1e-5.
+struct Team {
+    uint32_t S, t, sl;
+    bool active;
+};
+__device__ __forceinline__ Team make_team(uint32_t nt, uint32_t lane) {
+    Team tm;
+    const float inv = __frcp_rn((float)nt);
+    tm.S = (uint32_t)(32.5f * inv);
+    tm.sl = (uint32_t)(((float)lane + 0.5f) * inv);
+    tm.t = lane - tm.sl * nt;
+    tm.active = tm.sl < tm.S;
+    return tm;
 }
 
 // Sum v over the S slices of each target (lanes t + s*nt); the total lands in slice 0.
@@ -64,6 +144,24 @@ __device__ __forceinline__ T slice_sum(T v, uint32_t S, uint32_t nt, uint32_t sl
     }
     return v;
 }
+
+// Bit strings: a chunk of nt <= 32 targets with L staged candidates gives each lane
+// IT = ceil(ceil(L/2) / S) pair iterations, packed 16 per 32-bit word. A target's words live in
+// its slot hits[ti * MASK_WORDS + w * S + sl] when nwords * S fits the slot.
+struct MaskShape {
+    uint32_t IT, nwords;
+    bool ok;
+};
+__device__ __forceinline__ MaskShape mask_shape(uint32_t total, uint32_t S, bool single_chunk) {
+    MaskShape ms;
+    const uint32_t pairs = (total + 1u) >> 1;
+    ms.IT = (pairs + S - 1u) / S;
+    ms.nwords = (ms.IT + 15u) >> 4;
+    ms.ok = single_chunk && total + 64u <= (uint32_t)STAGE_CAP && ms.nwords * S <= (uint32_t)MASK_WORDS;
+    return ms;
+}
+
+// ---- reference-only terms ---------------------------------------------------------------------
 
 // density.comp:53-55 evaluated as the reference does, for the wall term.
 __device__ __forceinline__ float poly6_ref(const SceneConsts& c, float r) {
@@ -89,7 +187,7 @@ __device__ void wall_forces(const SceneConsts& c, const float p[3], float f[3]) 
     const float s = (c.h - 3.f) * (c.h - 3.f);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float target;
+        float target = 0.f;
         bool hit = false;
         if (p[a] < c.h) { target = 0.f; hit = true; }
         else if (p[a] > c.size - c.h) { target = c.size; hit = true; }
@@ -129,151 +227,312 @@ __device__ void mouse_force(const SceneConsts& c, const StepInputs& in, const fl
     for (int a = 0; a < 3; ++a) f[a] = (k * ((s * (tm[a] / dd)) * c.cs));
 }
 
-__global__ void __launch_bounds__(SPH_THREADS) density_kernel(const SceneConsts sc, const uint32_t n,
-                                                              const float4* __restrict__ pos_in,
-                                                              float* rho_out,  // aliases pos_in[].w
-                                                              float* p_out,    // aliases vel[].w
-                                                              const uint32_t* __restrict__ start,
-                                                              const uint32_t* __restrict__ cell_list,
-                                                              const uint32_t* __restrict__ num_nonempty,
-                                                              uint32_t* __restrict__ ncount) {
+__device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, uint32_t hits, const float4& pi,
+                                              uint32_t ti, float* rho_out, float* p_out, uint32_t* ncount) {
+    // The sum includes the particle itself (w = h^2): the reference's m*W(0) term.
+    const float rho = (sc.m * sc.c6) * sum;
+    float pressure;
+    if (sc.eos == WC_EOS_LINEAR) {
+        pressure = sc.p0 + sc.k * (rho - sc.rho0);
+    } else {
+        const float x = rho / sc.rho0;
+        pressure = sc.p0 + sc.k * (x * x * x - 1.f);
+    }
+    float total = rho;
+    if (sc.flags & WC_FLAG_WALL_DENSITY) total = rho + wall_density(sc, pi.x, pi.y, pi.z);
+    rho_out[4 * (size_t)ti] = total;
+    p_out[4 * (size_t)ti] = pressure;
+    if (ncount) ncount[ti] = hits - 1u;
+}
+
+// ---- density --------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(SPH_THREADS, 6) density_kernel(const SceneConsts sc, const uint32_t n,
+                                                                 const float4* __restrict__ pos_in,
+                                                                 float* rho_out,  // aliases pos_in[].w
+                                                                 float* p_out,    // aliases vel[].w
+                                                                 const uint32_t* __restrict__ start,
+                                                                 const uint32_t* __restrict__ cell_list,
+                                                                 const uint32_t* __restrict__ num_nonempty,
+                                                                 uint32_t* __restrict__ ncount,
+                                                                 uint32_t* __restrict__ hits) {
+    __shared__ __align__(16) float s_stage[WARPS][3][STAGE_CAP];
     const uint32_t lane = threadIdx.x & 31u;
+    float* sx = s_stage[threadIdx.x >> 5][0];
+    float* sy = s_stage[threadIdx.x >> 5][1];
+    float* sz = s_stage[threadIdx.x >> 5][2];
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t M = min(*num_nonempty, (uint32_t)sc.R * (uint32_t)sc.R * (uint32_t)sc.R);
-    const int32_t R = sc.R;
+    const f2 h2x2 = pk(sc.h2, sc.h2);
     for (uint32_t m = warp; m < M; m += nwarps) {
-        const uint32_t c = __ldg(cell_list + m);
-        const uint32_t cend = min(__ldg(start + c + 1), n), cbeg = min(__ldg(start + c), cend);
-        const int cx = (int)(c % (uint32_t)R), cy = (int)((c / (uint32_t)R) % (uint32_t)R),
-                  cz = (int)(c / ((uint32_t)R * R));
-        uint32_t rlo, rhi;
-        row_range(start, n, R, cx, cy, cz, lane, rlo, rhi);
-        for (uint32_t t0 = cbeg; t0 < cend; t0 += 32u) {
-            const uint32_t nt = min(32u, cend - t0);
-            const uint32_t S = 32u / nt;
-            const uint32_t t = lane % nt, sl = lane / nt;
-            const bool active = sl < S;
-            const uint32_t ti = t0 + t;
-            const float4 pi = pos_in[ti];
-            float sum = 0.f;
-            uint32_t cnt = 0;
+        const CellRows cr = cell_rows(start, n, sc.R, __ldg(cell_list + m), lane);
+        if (cr.total + 64u <= (uint32_t)STAGE_CAP) {
+            // Stage: the concatenated candidate list as x/y/z arrays, then 64 far-away entries
+            // (a lane's last pair may run up to 63 past the end; their d2 overflows to +inf).
 #pragma unroll 1
             for (int r = 0; r < 9; ++r) {
-                const uint32_t lo = __shfl_sync(FULL, rlo, r), hi = __shfl_sync(FULL, rhi, r);
-                if (!active) continue;
-#pragma unroll 4
-                for (uint32_t k = lo + sl; k < hi; k += S) {
-                    const float4 pj = __ldg(pos_in + k);
-                    const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
-                    if (d2 <= sc.cull) {
-                        const float w = sc.h2 - d2;
-                        sum = fmaf(w * w, w, sum);
-                        ++cnt;
-                    }
+                const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
+                const uint32_t len = __shfl_sync(FULL, cr.len, r);
+                const uint32_t base = __shfl_sync(FULL, cr.pex, r);
+                for (uint32_t j = lane; j < len; j += 32u) {
+                    const float4 v = __ldg(pos_in + lo + j);
+                    sx[base + j] = v.x;
+                    sy[base + j] = v.y;
+                    sz[base + j] = v.z;
                 }
             }
-            sum = slice_sum(sum, S, nt, sl);
-            cnt = slice_sum(cnt, S, nt, sl);
-            if (sl == 0u) {
-                // The sum includes the particle itself (w = h^2): the reference's m*W(0) term.
-                const float rho = (sc.m * sc.c6) * sum;
-                float pressure;
-                if (sc.eos == WC_EOS_LINEAR) {
-                    pressure = sc.p0 + sc.k * (rho - sc.rho0);
-                } else {
-                    const float x = rho / sc.rho0;
-                    pressure = sc.p0 + sc.k * (x * x * x - 1.f);
+            sx[cr.total + lane] = 1e30f;
+            sy[cr.total + lane] = 1e30f;
+            sz[cr.total + lane] = 1e30f;
+            sx[cr.total + 32u + lane] = 1e30f;
+            sy[cr.total + 32u + lane] = 1e30f;
+            sz[cr.total + 32u + lane] = 1e30f;
+            __syncwarp();
+            const bool single = cr.cend - cr.cbeg <= 32u;
+            for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
+                const uint32_t nt = min(32u, cr.cend - t0);
+                const Team tm = make_team(nt, lane);
+                const MaskShape ms = mask_shape(cr.total, tm.S, single);
+                const bool store = ms.ok && hits != nullptr && tm.active;
+                const uint32_t ti = t0 + tm.t;
+                const float4 pi = pos_in[ti];
+                const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
+                f2 acc = pk(0.f, 0.f);
+                uint32_t nh = 0, it = 0;
+                for (uint32_t w = 0; w < ms.nwords; ++w) {
+                    uint32_t word = 0;
+                    const uint32_t jend = min(16u, ms.IT - 16u * w);
+#pragma unroll 4
+                    for (uint32_t j = 0; j < jend; ++j, ++it) {
+                        const uint32_t q = 2u * (it * tm.S + tm.sl);
+                        const f2 x2 = *reinterpret_cast<const f2*>(sx + q);
+                        const f2 y2 = *reinterpret_cast<const f2*>(sy + q);
+                        const f2 z2 = *reinterpret_cast<const f2*>(sz + q);
+                        const f2 dx = sub2(px, x2), dy = sub2(py, y2), dz = sub2(pz, z2);
+                        const f2 d2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+                        float d0, d1;
+                        upk(d2, d0, d1);
+                        const bool h0 = d0 <= sc.cull, h1 = d1 <= sc.cull;
+                        const f2 wv = sub2(h2x2, d2);
+                        float a0, a1;
+                        upk(mul2(mul2(wv, wv), wv), a0, a1);
+                        acc = add2(acc, pk(h0 ? a0 : 0.f, h1 ? a1 : 0.f));
+                        word |= ((uint32_t)h0 | ((uint32_t)h1 << 1)) << (2u * j);
+                    }
+                    nh += __popc(word);
+                    if (store) hits[(size_t)ti * MASK_WORDS + w * tm.S + tm.sl] = word;
                 }
-                float total = rho;
-                if (sc.flags & WC_FLAG_WALL_DENSITY) total = rho + wall_density(sc, pi.x, pi.y, pi.z);
-                rho_out[4 * (size_t)ti] = total;
-                p_out[4 * (size_t)ti] = pressure;
-                if (ncount) ncount[ti] = cnt - 1u;
+                float a0, a1;
+                upk(acc, a0, a1);
+                float sum = a0 + a1;
+                if (!tm.active) {
+                    sum = 0.f;
+                    nh = 0;
+                }
+                sum = slice_sum(sum, tm.S, nt, tm.sl);
+                nh = slice_sum(nh, tm.S, nt, tm.sl);
+                if (tm.sl == 0u) write_density(sc, sum, nh, pi, ti, rho_out, p_out, ncount);
+            }
+            __syncwarp();  // the stage is rewritten for the next cell
+        } else {
+            // Direct path: candidates straight from global memory (no bit strings).
+            for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
+                const uint32_t nt = min(32u, cr.cend - t0);
+                const Team tm = make_team(nt, lane);
+                const uint32_t ti = t0 + tm.t;
+                const float4 pi = pos_in[ti];
+                float sum = 0.f;
+                uint32_t cnt = 0;
+#pragma unroll 1
+                for (int r = 0; r < 9; ++r) {
+                    const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
+                    const uint32_t hi = lo + __shfl_sync(FULL, cr.len, r);
+                    if (!tm.active) continue;
+                    for (uint32_t k = lo + tm.sl; k < hi; k += tm.S) {
+                        const float4 pj = __ldg(pos_in + k);
+                        const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+                        if (d2 <= sc.cull) {
+                            const float w = sc.h2 - d2;
+                            sum = fmaf(w * w, w, sum);
+                            ++cnt;
+                        }
+                    }
+                }
+                sum = slice_sum(sum, tm.S, nt, tm.sl);
+                cnt = slice_sum(cnt, tm.S, nt, tm.sl);
+                if (tm.sl == 0u) write_density(sc, sum, cnt, pi, ti, rho_out, p_out, ncount);
             }
         }
     }
 }
 
-template <int CAP>
+// ---- force + integration ------------------------------------------------------------------------
+
+// One neighbour's pressure and viscosity terms. f[0..2] collects pres*(h-d)^2*r/d and f[3..5]
+// collects (v_j - v_i)*(h-d)/rho_j; the constant factors are applied once per particle.
+__device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, const float4& pj, const float4& vj,
+                                           float h, float f[6]) {
+    const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+    const float d2 = dist2(rx, ry, rz);
+    const float rsq = d2 > 0.f ? rsqrtf(d2) : 0.f;  // coincident pair (or self): r = 0, no push
+    const float d = d2 * rsq;
+    const float inv_rho = __frcp_rn(pj.w);
+    const float hd = h - d;
+    const float pres = (vi.w + vj.w) * (0.5f * inv_rho);  // (p_i + p_j) / (2 rho_j)
+    if (pres > 0.f) {
+        const float coef = pres * hd * hd * rsq;
+        f[0] = fmaf(coef, rx, f[0]);
+        f[1] = fmaf(coef, ry, f[1]);
+        f[2] = fmaf(coef, rz, f[2]);
+    }
+    const float wv = hd * inv_rho;
+    f[3] = fmaf(vj.x - vi.x, wv, f[3]);
+    f[4] = fmaf(vj.y - vi.y, wv, f[4]);
+    f[5] = fmaf(vj.z - vi.z, wv, f[5]);
+}
+
 __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t cnt, uint32_t lane, const float4& pi,
                                                 const float4& vi, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vel, float h, float f[6]) {
     for (uint32_t e = 0; e < cnt; ++e) {
         const uint32_t k = list[e * 32u + lane];
-        const float4 pj = __ldg(pos + k);
-        const float4 vj = __ldg(vel + k);
-        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float d2 = dist2(rx, ry, rz);
-        const float rsq = d2 > 0.f ? rsqrtf(d2) : 0.f;  // coincident pair: r = 0, no pressure push
-        const float d = d2 * rsq;
-        const float inv_rho = __frcp_rn(pj.w);
-        const float hd = h - d;
-        const float pres = (vi.w + vj.w) * (0.5f * inv_rho);  // (p_i + p_j) / (2 rho_j)
-        if (pres > 0.f) {
-            const float coef = pres * hd * hd * rsq;
-            f[0] = fmaf(coef, rx, f[0]);
-            f[1] = fmaf(coef, ry, f[1]);
-            f[2] = fmaf(coef, rz, f[2]);
-        }
-        const float wv = hd * inv_rho;
-        f[3] = fmaf(vj.x - vi.x, wv, f[3]);
-        f[4] = fmaf(vj.y - vi.y, wv, f[4]);
-        f[5] = fmaf(vj.z - vi.z, wv, f[5]);
+        pair_terms(pi, vi, __ldg(pos + k), __ldg(vel + k), h, f);
     }
 }
 
-template <int CAP>
-__global__ void __launch_bounds__(SPH_THREADS) force_kernel(const SceneConsts sc, const StepInputs in, const uint32_t n,
-                                                            const float4* __restrict__ pos_b,
-                                                            const float4* __restrict__ vel_b,
-                                                            const uint32_t* __restrict__ ids_b,
-                                                            float4* __restrict__ pos_a, float4* __restrict__ vel_a,
-                                                            uint32_t* __restrict__ ids_a,
-                                                            const uint32_t* __restrict__ start,
-                                                            const uint32_t* __restrict__ cell_list,
-                                                            const uint32_t* __restrict__ num_nonempty) {
-    extern __shared__ uint32_t s_lists[];
+// Gravity, reference-only external terms, symplectic Euler, speed clamp and wall collision
+// (update.comp:145,191-231), then the store into the state buffer.
+__device__ __forceinline__ void integrate_store(const SceneConsts& sc, const StepInputs& in, const float4& pi,
+                                                const float4& vi, const float f[6], uint32_t ti,
+                                                float4* __restrict__ pos_a, float4* __restrict__ vel_a,
+                                                const uint32_t* __restrict__ ids_b, uint32_t* __restrict__ ids_a) {
+    const float fp_scale = -sc.m * sc.cs;         // -m * spiky const
+    const float fv_scale = sc.m * sc.cv * sc.mu;  // m * visc const * mu
+    const float rho = pi.w, pressure = vi.w;
+    const float p3[3] = {pi.x, pi.y, pi.z};
+    float ext[3] = {in.g[0] * rho, in.g[1] * rho, in.g[2] * rho};
+    if (sc.flags & (WC_FLAG_WALL_FORCE | WC_FLAG_MOUSE_FORCE)) {
+        float wf[3] = {0.f, 0.f, 0.f}, mf[3] = {0.f, 0.f, 0.f};
+        if (sc.flags & WC_FLAG_WALL_FORCE) wall_forces(sc, p3, wf);
+        if (sc.flags & WC_FLAG_MOUSE_FORCE) mouse_force(sc, in, p3, pressure, mf);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) ext[a] += mf[a] + wf[a];
+    }
+    const float inv = 1.f / (rho + 1e-16f);
+    const float vin[3] = {vi.x, vi.y, vi.z};
+    float v[3], x[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float force = fp_scale * f[a] + fv_scale * f[3 + a] + ext[a];
+        float va = vin[a] + (force * inv) * in.dt;
+        if (sc.flags & WC_FLAG_SPEED_CLAMP) va = fminf(fmaxf(va, -sc.max_speed), sc.max_speed);
+        float xa = p3[a] + va * in.dt;
+        if (xa < sc.border) {
+            va *= -sc.damping;
+            xa = sc.border;
+        } else if (xa > sc.size - sc.border) {
+            va *= -sc.damping;
+            xa = sc.size - sc.border;
+        }
+        v[a] = va;
+        x[a] = xa;
+    }
+    pos_a[ti] = make_float4(x[0], x[1], x[2], rho);
+    vel_a[ti] = make_float4(v[0], v[1], v[2], pressure);
+    if (ids_a) ids_a[ti] = ids_b[ti];
+}
+
+__global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts sc, const StepInputs in,
+                                                               const uint32_t n, const float4* __restrict__ pos_b,
+                                                               const float4* __restrict__ vel_b,
+                                                               const uint32_t* __restrict__ ids_b,
+                                                               float4* __restrict__ pos_a, float4* __restrict__ vel_a,
+                                                               uint32_t* __restrict__ ids_a,
+                                                               const uint32_t* __restrict__ start,
+                                                               const uint32_t* __restrict__ cell_list,
+                                                               const uint32_t* __restrict__ num_nonempty,
+                                                               const uint32_t* __restrict__ hits) {
+    __shared__ uint32_t s_slot[WARPS][STAGE_CAP];             // candidate number -> sorted slot
+    __shared__ uint32_t s_lists[WARPS][FORCE_LIST_CAP * 32];  // direct path: per-lane lists
     const uint32_t lane = threadIdx.x & 31u;
-    uint32_t* list = s_lists + (threadIdx.x >> 5) * (CAP * 32);
+    uint32_t* slot = s_slot[threadIdx.x >> 5];
+    uint32_t* list = s_lists[threadIdx.x >> 5];
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t M = min(*num_nonempty, (uint32_t)sc.R * (uint32_t)sc.R * (uint32_t)sc.R);
-    const int32_t R = sc.R;
-    const float fp_scale = -sc.m * sc.cs;           // -m * spiky const
-    const float fv_scale = sc.m * sc.cv * sc.mu;    // m * visc const * mu
     for (uint32_t m = warp; m < M; m += nwarps) {
-        const uint32_t c = __ldg(cell_list + m);
-        const uint32_t cend = min(__ldg(start + c + 1), n), cbeg = min(__ldg(start + c), cend);
-        const int cx = (int)(c % (uint32_t)R), cy = (int)((c / (uint32_t)R) % (uint32_t)R),
-                  cz = (int)(c / ((uint32_t)R * R));
-        uint32_t rlo, rhi;
-        row_range(start, n, R, cx, cy, cz, lane, rlo, rhi);
-        for (uint32_t t0 = cbeg; t0 < cend; t0 += 32u) {
-            const uint32_t nt = min(32u, cend - t0);
-            const uint32_t S = 32u / nt;
-            const uint32_t t = lane % nt, sl = lane / nt;
-            const bool active = sl < S;
-            const uint32_t ti = t0 + t;
+        const CellRows cr = cell_rows(start, n, sc.R, __ldg(cell_list + m), lane);
+        const uint32_t ncell = cr.cend - cr.cbeg;
+        bool replay = false;
+        if (ncell <= 32u && hits != nullptr) {
+            const Team tm = make_team(ncell, lane);
+            replay = mask_shape(cr.total, tm.S, true).ok;
+        }
+        if (replay) {
+            // Replay the density pass's bit strings: same team, same candidate numbering.
+#pragma unroll 1
+            for (int r = 0; r < 9; ++r) {
+                const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
+                const uint32_t len = __shfl_sync(FULL, cr.len, r);
+                const uint32_t base = __shfl_sync(FULL, cr.pex, r);
+                for (uint32_t j = lane; j < len; j += 32u) slot[base + j] = lo + j;
+            }
+            __syncwarp();
+            const uint32_t nt = ncell;
+            const Team tm = make_team(nt, lane);
+            const MaskShape ms = mask_shape(cr.total, tm.S, true);
+            const uint32_t ti = cr.cbeg + tm.t;
+            const float4 pi = pos_b[ti];
+            const float4 vi = vel_b[ti];
+            float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (tm.active) {
+                for (uint32_t w = 0; w < ms.nwords; ++w) {
+                    uint32_t word = __ldg(hits + (size_t)ti * MASK_WORDS + w * tm.S + tm.sl);
+                    while (word) {
+                        const uint32_t b = (uint32_t)__ffs(word) - 1u;
+                        word &= word - 1u;
+                        const uint32_t it = 16u * w + (b >> 1);
+                        const uint32_t q = 2u * (it * tm.S + tm.sl) + (b & 1u);
+                        // Bits always come from this step's density pass over the same tables;
+                        // the checks only keep a stage-by-stage caller's stale bits in bounds.
+                        if (q >= cr.total) continue;
+                        const uint32_t k = slot[q];
+                        if (k >= n) continue;
+                        pair_terms(pi, vi, __ldg(pos_b + k), __ldg(vel_b + k), sc.h, f);
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
+            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a);
+            __syncwarp();  // the slot table is rewritten for the next cell
+            continue;
+        }
+        // Direct path: cull every candidate into per-lane shared-memory lists, then evaluate.
+        for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
+            const uint32_t nt = min(32u, cr.cend - t0);
+            const Team tm = make_team(nt, lane);
+            const uint32_t ti = t0 + tm.t;
             const float4 pi = pos_b[ti];
             const float4 vi = vel_b[ti];
             float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             uint32_t cnt = 0;
 #pragma unroll 1
             for (int r = 0; r < 9; ++r) {
-                const uint32_t lo = __shfl_sync(FULL, rlo, r), hi = __shfl_sync(FULL, rhi, r);
-                const uint32_t iters = (hi - lo + S - 1u) / S;
-                for (uint32_t seg = 0; seg < iters; seg += CAP) {
-                    const uint32_t seg_iters = min((uint32_t)CAP, iters - seg);
-                    if (__any_sync(FULL, cnt + seg_iters > (uint32_t)CAP)) {
-                        accumulate_list<CAP>(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
+                const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
+                const uint32_t hi = lo + __shfl_sync(FULL, cr.len, r);
+                const uint32_t iters = (hi - lo + tm.S - 1u) / tm.S;
+                for (uint32_t seg = 0; seg < iters; seg += FORCE_LIST_CAP) {
+                    const uint32_t seg_iters = min((uint32_t)FORCE_LIST_CAP, iters - seg);
+                    if (__any_sync(FULL, cnt + seg_iters > (uint32_t)FORCE_LIST_CAP)) {
+                        accumulate_list(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
                         cnt = 0;
                     }
-                    if (active) {
-                        const uint32_t k0 = lo + seg * S + sl;
-#pragma unroll 4
+                    if (tm.active) {
+                        const uint32_t k0 = lo + seg * tm.S + tm.sl;
                         for (uint32_t it = 0; it < seg_iters; ++it) {
-                            const uint32_t k = k0 + it * S;
+                            const uint32_t k = k0 + it * tm.S;
                             if (k < hi) {
                                 const float4 pj = __ldg(pos_b + k);
                                 const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
@@ -284,48 +543,13 @@ __global__ void __launch_bounds__(SPH_THREADS) force_kernel(const SceneConsts sc
                     }
                 }
             }
-            accumulate_list<CAP>(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
+            accumulate_list(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
 #pragma unroll
-            for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], S, nt, sl);
-            if (sl == 0u) {
-                const float rho = pi.w, pressure = vi.w;
-                const float p3[3] = {pi.x, pi.y, pi.z};
-                float ext[3] = {in.g[0] * rho, in.g[1] * rho, in.g[2] * rho};
-                if (sc.flags & (WC_FLAG_WALL_FORCE | WC_FLAG_MOUSE_FORCE)) {
-                    float wf[3] = {0.f, 0.f, 0.f}, mf[3] = {0.f, 0.f, 0.f};
-                    if (sc.flags & WC_FLAG_WALL_FORCE) wall_forces(sc, p3, wf);
-                    if (sc.flags & WC_FLAG_MOUSE_FORCE) mouse_force(sc, in, p3, pressure, mf);
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) ext[a] += mf[a] + wf[a];
-                }
-                const float inv = 1.f / (rho + 1e-16f);
-                const float vin[3] = {vi.x, vi.y, vi.z};
-                float v[3], x[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const float force = fp_scale * f[a] + fv_scale * f[3 + a] + ext[a];
-                    float va = vin[a] + (force * inv) * in.dt;
-                    if (sc.flags & WC_FLAG_SPEED_CLAMP) va = fminf(fmaxf(va, -sc.max_speed), sc.max_speed);
-                    float xa = p3[a] + va * in.dt;
-                    if (xa < sc.border) {
-                        va *= -sc.damping;
-                        xa = sc.border;
-                    } else if (xa > sc.size - sc.border) {
-                        va *= -sc.damping;
-                        xa = sc.size - sc.border;
-                    }
-                    v[a] = va;
-                    x[a] = xa;
-                }
-                pos_a[ti] = make_float4(x[0], x[1], x[2], rho);
-                vel_a[ti] = make_float4(v[0], v[1], v[2], pressure);
-                if (ids_a) ids_a[ti] = ids_b[ti];
-            }
+            for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
+            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a);
         }
     }
 }
-
-constexpr size_t force_smem_bytes() { return (size_t)(SPH_THREADS / 32) * FORCE_LIST_CAP * 32 * sizeof(uint32_t); }
 
 }  // namespace
 
@@ -335,7 +559,7 @@ LaunchDims compute_launch_dims(int device) {
     if (ld.sms <= 0) ld.sms = 1;
     int bd = 0, bf = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel, SPH_THREADS, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<FORCE_LIST_CAP>, SPH_THREADS, force_smem_bytes());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel, SPH_THREADS, 0);
     ld.grid_density = ld.sms * (bd > 0 ? bd : 1);
     ld.grid_force = ld.sms * (bf > 0 ? bf : 1);
     ld.grid_stream = ld.sms * 8;
@@ -345,15 +569,15 @@ LaunchDims compute_launch_dims(int device) {
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s) {
     density_kernel<<<ld.grid_density, SPH_THREADS, 0, s>>>(
         sc, d.n, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3, reinterpret_cast<float*>(d.vel_b) + 3, d.start,
-        d.cell_list, d.num_nonempty, (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr);
+        d.cell_list, d.num_nonempty, (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr, d.hits);
 }
 
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s) {
-    force_kernel<FORCE_LIST_CAP><<<ld.grid_force, SPH_THREADS, force_smem_bytes(), s>>>(
-        sc, in, d.n, d.pos_b, d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start, d.cell_list, d.num_nonempty);
+    force_kernel<<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, in, d.n, d.pos_b, d.vel_b, d.ids_b, d.pos_a, d.vel_a,
+                                                       d.ids_a, d.start, d.cell_list, d.num_nonempty, d.hits);
 }
 
-const void* force_kernel_symbol(uint32_t) { return reinterpret_cast<const void*>(&force_kernel<FORCE_LIST_CAP>); }
+const void* force_kernel_symbol(uint32_t) { return reinterpret_cast<const void*>(&force_kernel); }
 
 }  // namespace wc
