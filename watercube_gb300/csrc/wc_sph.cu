@@ -15,10 +15,11 @@
 // so every lane runs the same trip count. Partial sums are combined with shuffles in a fixed
 // order: results are deterministic.
 //
-// Density: the candidates' positions are staged in shared memory as x/y/z arrays and tested two
-// at a time with Blackwell's packed f32x2 FMA (one instruction updates both candidates). Each
-// lane records which of its candidates passed as a bit string (2 bits per pair); the force pass
-// replays exactly those bits instead of testing all candidates again. Cells whose candidate
+// Density: the candidates' positions are staged in shared memory as x/y/z arrays and tested four
+// at a time (one 128-bit shared load per coordinate) with Blackwell's packed f32x2 arithmetic
+// (one instruction updates two candidates). Each lane records which of its candidates passed
+// as a bit string; the force pass replays exactly those bits, gathering four neighbours per
+// round, instead of testing all candidates again. Cells whose candidate
 // list does not fit the stage, cells of more than 32 particles and bit strings longer than the
 // per-particle slot take the direct path: the density pass reads candidates from global memory
 // and the force pass culls into a per-lane shared-memory list.
@@ -145,20 +146,32 @@ __device__ __forceinline__ T slice_sum(T v, uint32_t S, uint32_t nt, uint32_t sl
     return v;
 }
 
-// Bit strings: a chunk of nt <= 32 targets with L staged candidates gives each lane
-// IT = ceil(ceil(L/2) / S) pair iterations, packed 16 per 32-bit word. A target's words live in
-// its slot hits[ti * MASK_WORDS + w * S + sl] when nwords * S fits the slot.
+// Staged candidates are tested four at a time: slice sl of a target takes quads sl, sl+S, ...
+// (candidates 4q .. 4q+3), so a chunk of targets split S ways runs IT = ceil(ceil(L/4) / S)
+// iterations and reads up to 4*S + 8 entries past the list; those entries hold far-away
+// positions. Bit strings pack 8 iterations (32 candidates) per 32-bit word; a target's words
+// live in its slot hits[ti * MASK_WORDS + w * S + sl] when nwords * S fits the slot.
+__device__ __forceinline__ uint32_t stage_padding(uint32_t S) { return 4u * S + 8u; }
+
 struct MaskShape {
     uint32_t IT, nwords;
     bool ok;
 };
 __device__ __forceinline__ MaskShape mask_shape(uint32_t total, uint32_t S, bool single_chunk) {
     MaskShape ms;
-    const uint32_t pairs = (total + 1u) >> 1;
-    ms.IT = (pairs + S - 1u) / S;
-    ms.nwords = (ms.IT + 15u) >> 4;
-    ms.ok = single_chunk && total + 64u <= (uint32_t)STAGE_CAP && ms.nwords * S <= (uint32_t)MASK_WORDS;
+    const uint32_t quads = (total + 3u) >> 2;
+    ms.IT = (quads + S - 1u) / S;
+    ms.nwords = (ms.IT + 7u) >> 3;
+    ms.ok = single_chunk && total + stage_padding(S) <= (uint32_t)STAGE_CAP &&
+            ms.nwords * S <= (uint32_t)MASK_WORDS;
     return ms;
+}
+
+// The split of the last (smallest) chunk of a cell has the most slices, hence the most padding.
+__device__ __forceinline__ uint32_t max_slices(uint32_t ncell) {
+    const uint32_t rem = ncell & 31u;
+    const uint32_t last = rem ? rem : 32u;
+    return 32u / last;
 }
 
 // ---- reference-only terms ---------------------------------------------------------------------
@@ -247,7 +260,7 @@ __device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, 
 
 // ---- density --------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(SPH_THREADS, 6) density_kernel(const SceneConsts sc, const uint32_t n,
+__global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneConsts sc, const uint32_t n,
                                                                  const float4* __restrict__ pos_in,
                                                                  float* rho_out,  // aliases pos_in[].w
                                                                  float* p_out,    // aliases vel[].w
@@ -264,12 +277,13 @@ __global__ void __launch_bounds__(SPH_THREADS, 6) density_kernel(const SceneCons
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t M = min(*num_nonempty, (uint32_t)sc.R * (uint32_t)sc.R * (uint32_t)sc.R);
-    const f2 h2x2 = pk(sc.h2, sc.h2);
+    const f2 cull2 = pk(sc.cull, sc.cull);
     for (uint32_t m = warp; m < M; m += nwarps) {
         const CellRows cr = cell_rows(start, n, sc.R, __ldg(cell_list + m), lane);
-        if (cr.total + 64u <= (uint32_t)STAGE_CAP) {
-            // Stage: the concatenated candidate list as x/y/z arrays, then 64 far-away entries
-            // (a lane's last pair may run up to 63 past the end; their d2 overflows to +inf).
+        const uint32_t pad = stage_padding(max_slices(cr.cend - cr.cbeg));
+        if (cr.total + pad <= (uint32_t)STAGE_CAP) {
+            // Stage: the concatenated candidate list as x/y/z arrays, then `pad` far-away
+            // entries (their d2 overflows to +inf, so they never pass).
 #pragma unroll 1
             for (int r = 0; r < 9; ++r) {
                 const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
@@ -282,12 +296,11 @@ __global__ void __launch_bounds__(SPH_THREADS, 6) density_kernel(const SceneCons
                     sz[base + j] = v.z;
                 }
             }
-            sx[cr.total + lane] = 1e30f;
-            sy[cr.total + lane] = 1e30f;
-            sz[cr.total + lane] = 1e30f;
-            sx[cr.total + 32u + lane] = 1e30f;
-            sy[cr.total + 32u + lane] = 1e30f;
-            sz[cr.total + 32u + lane] = 1e30f;
+            for (uint32_t j = lane; j < pad; j += 32u) {
+                sx[cr.total + j] = 1e30f;
+                sy[cr.total + j] = 1e30f;
+                sz[cr.total + j] = 1e30f;
+            }
             __syncwarp();
             const bool single = cr.cend - cr.cbeg <= 32u;
             for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
@@ -298,34 +311,45 @@ __global__ void __launch_bounds__(SPH_THREADS, 6) density_kernel(const SceneCons
                 const uint32_t ti = t0 + tm.t;
                 const float4 pi = pos_in[ti];
                 const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
-                f2 acc = pk(0.f, 0.f);
+                // Quads are 16-byte aligned: q is a multiple of 4 floats.
+                const float4* bx = reinterpret_cast<const float4*>(sx) + tm.sl;
+                const float4* by = reinterpret_cast<const float4*>(sy) + tm.sl;
+                const float4* bz = reinterpret_cast<const float4*>(sz) + tm.sl;
+                f2 acc01 = pk(0.f, 0.f), acc23 = pk(0.f, 0.f);
                 uint32_t nh = 0, it = 0;
                 for (uint32_t w = 0; w < ms.nwords; ++w) {
                     uint32_t word = 0;
-                    const uint32_t jend = min(16u, ms.IT - 16u * w);
-#pragma unroll 4
+                    const uint32_t jend = min(8u, ms.IT - 8u * w);
+#pragma unroll 2
                     for (uint32_t j = 0; j < jend; ++j, ++it) {
-                        const uint32_t q = 2u * (it * tm.S + tm.sl);
-                        const f2 x2 = *reinterpret_cast<const f2*>(sx + q);
-                        const f2 y2 = *reinterpret_cast<const f2*>(sy + q);
-                        const f2 z2 = *reinterpret_cast<const f2*>(sz + q);
-                        const f2 dx = sub2(px, x2), dy = sub2(py, y2), dz = sub2(pz, z2);
-                        const f2 d2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-                        float d0, d1;
-                        upk(d2, d0, d1);
-                        const bool h0 = d0 <= sc.cull, h1 = d1 <= sc.cull;
-                        const f2 wv = sub2(h2x2, d2);
-                        float a0, a1;
-                        upk(mul2(mul2(wv, wv), wv), a0, a1);
-                        acc = add2(acc, pk(h0 ? a0 : 0.f, h1 ? a1 : 0.f));
-                        word |= ((uint32_t)h0 | ((uint32_t)h1 << 1)) << (2u * j);
+                        const uint32_t qd = it * tm.S;
+                        const float4 X = bx[qd], Y = by[qd], Z = bz[qd];
+                        const f2 dx01 = sub2(px, pk(X.x, X.y)), dx23 = sub2(px, pk(X.z, X.w));
+                        const f2 dy01 = sub2(py, pk(Y.x, Y.y)), dy23 = sub2(py, pk(Y.z, Y.w));
+                        const f2 dz01 = sub2(pz, pk(Z.x, Z.y)), dz23 = sub2(pz, pk(Z.z, Z.w));
+                        const f2 d01 = fma2(dz01, dz01, fma2(dy01, dy01, mul2(dx01, dx01)));
+                        const f2 d23 = fma2(dz23, dz23, fma2(dy23, dy23, mul2(dx23, dx23)));
+                        // u = cull - d2 >= 0 exactly when d2 <= cull (a tie gives +0): the
+                        // sign bits are the misses.
+                        float u0, u1, u2, u3;
+                        upk(sub2(cull2, d01), u0, u1);
+                        upk(sub2(cull2, d23), u2, u3);
+                        const uint32_t miss = (__float_as_uint(u0) >> 31) | ((__float_as_uint(u1) >> 31) << 1) |
+                                              ((__float_as_uint(u2) >> 31) << 2) | ((__float_as_uint(u3) >> 31) << 3);
+                        word |= (~miss & 0xFu) << (4u * j);
+                        // Poly6 weight (cull - d2)^3 for hits, 0 otherwise (cull is h^2 to the ulp).
+                        const f2 w01 = pk(fmaxf(u0, 0.f), fmaxf(u1, 0.f));
+                        const f2 w23 = pk(fmaxf(u2, 0.f), fmaxf(u3, 0.f));
+                        acc01 = fma2(mul2(w01, w01), w01, acc01);
+                        acc23 = fma2(mul2(w23, w23), w23, acc23);
                     }
                     nh += __popc(word);
                     if (store) hits[(size_t)ti * MASK_WORDS + w * tm.S + tm.sl] = word;
                 }
-                float a0, a1;
-                upk(acc, a0, a1);
-                float sum = a0 + a1;
+                float a0, a1, a2, a3;
+                upk(acc01, a0, a1);
+                upk(acc23, a2, a3);
+                float sum = (a0 + a1) + (a2 + a3);
                 if (!tm.active) {
                     sum = 0.f;
                     nh = 0;
@@ -377,7 +401,7 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
     const float d2 = dist2(rx, ry, rz);
     const float rsq = d2 > 0.f ? rsqrtf(d2) : 0.f;  // coincident pair (or self): r = 0, no push
     const float d = d2 * rsq;
-    const float inv_rho = __frcp_rn(pj.w);
+    const float inv_rho = __fdividef(1.0f, pj.w);
     const float hd = h - d;
     const float pres = (vi.w + vj.w) * (0.5f * inv_rho);  // (p_i + p_j) / (2 rho_j)
     if (pres > 0.f) {
@@ -443,7 +467,7 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     if (ids_a) ids_a[ti] = ids_b[ti];
 }
 
-__global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts sc, const StepInputs in,
+__global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts sc, const StepInputs in,
                                                                const uint32_t n, const float4* __restrict__ pos_b,
                                                                const float4* __restrict__ vel_b,
                                                                const uint32_t* __restrict__ ids_b,
@@ -490,16 +514,33 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                 for (uint32_t w = 0; w < ms.nwords; ++w) {
                     uint32_t word = __ldg(hits + (size_t)ti * MASK_WORDS + w * tm.S + tm.sl);
                     while (word) {
-                        const uint32_t b = (uint32_t)__ffs(word) - 1u;
-                        word &= word - 1u;
-                        const uint32_t it = 16u * w + (b >> 1);
-                        const uint32_t q = 2u * (it * tm.S + tm.sl) + (b & 1u);
-                        // Bits always come from this step's density pass over the same tables;
-                        // the checks only keep a stage-by-stage caller's stale bits in bounds.
-                        if (q >= cr.total) continue;
-                        const uint32_t k = slot[q];
-                        if (k >= n) continue;
-                        pair_terms(pi, vi, __ldg(pos_b + k), __ldg(vel_b + k), sc.h, f);
+                        // Four neighbours per round so their loads overlap; empty places take
+                        // the particle itself, whose terms are exactly zero.
+                        uint32_t k[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            k[u] = ti;
+                            if (word) {
+                                const uint32_t b = (uint32_t)__ffs(word) - 1u;
+                                word &= word - 1u;
+                                const uint32_t q = 4u * ((8u * w + (b >> 2)) * tm.S + tm.sl) + (b & 3u);
+                                // Bits always come from this step's density pass over the same
+                                // tables; the checks only keep a stage-by-stage caller's stale
+                                // bits in bounds.
+                                if (q < cr.total) {
+                                    const uint32_t s = slot[q];
+                                    if (s < n) k[u] = s;
+                                }
+                            }
+                        }
+                        float4 pj[4], vj[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            pj[u] = __ldg(pos_b + k[u]);
+                            vj[u] = __ldg(vel_b + k[u]);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) pair_terms(pi, vi, pj[u], vj[u], sc.h, f);
                     }
                 }
             }
