@@ -242,6 +242,32 @@ WC_API const char* wc_step_kernel_name(uint32_t index);
 WC_API wc_status wc_fluid_time_steps(wc_fluid* f, float dt, uint32_t nsteps, int flush_l2, float* step_ms,
                                      float* kernel_ms);
 
+/* ---- cell sort without allocation ------------------------------------------------------ */
+
+#define WC_NOALLOC_MAX_PARTICLES (1u << 18) /* 262,144 */
+#define WC_NOALLOC_MAX_CELLS (1u << 18)     /* grid_res^3 <= 262,144, i.e. grid_res <= 64 */
+
+/*
+ * No counterpart in the reference. The cell sort of wc_fluid_sort (keys, stable permutation,
+ * cell table, positions gathered into sorted order) as one call that allocates no memory, for
+ * callers that cannot allocate when they sort: a frame loop where cudaMalloc would synchronise
+ * the GPU, or a host application that fixes its device memory budget up front. Its scratch is
+ * one fixed device array (about 8 MB) held by every GPU that loads the library, so it accepts
+ * at most WC_NOALLOC_MAX_PARTICLES particles and WC_NOALLOC_MAX_CELLS cells and rejects more
+ * with WC_ERR_INVALID_ARG. All buffers are device memory the caller owns:
+ *   d_positions        float4[n] (x, y, z, anything)        input
+ *   d_keys             uint32[n]   cell key per input particle
+ *   d_permutation      uint32[n]   sorted slot -> input index
+ *   d_cell_start       uint32[grid_res^3 + 1]  cell c holds slots [start[c], start[c+1])
+ *   d_sorted_positions float4[n]   positions in sorted order
+ * Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and not waited for. The
+ * first call on a device looks up the array's address and should come before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race, so order them on one stream.
+ */
+WC_API wc_status wc_sort_cells_noalloc(const void* d_positions, uint32_t n, uint32_t grid_res, float bin_size,
+                                       uint32_t* d_keys, uint32_t* d_permutation, uint32_t* d_cell_start,
+                                       void* d_sorted_positions, void* stream);
+
 /* Make `device` current for handles created afterwards on this thread (one process per GPU). */
 WC_API wc_status wc_set_device(int device);
 WC_API int wc_device_count(void);

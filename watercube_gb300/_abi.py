@@ -46,6 +46,9 @@ WC_UINTS_CELL_OFFSETS = 4
 WC_UINTS_NEIGHBOR_COUNTS = 5
 WC_UINTS_PARTICLE_IDS = 6
 
+WC_NOALLOC_MAX_PARTICLES = 1 << 18
+WC_NOALLOC_MAX_CELLS = 1 << 18
+
 
 class WatercubeError(RuntimeError):
     def __init__(self, status: int, message: str):
@@ -155,6 +158,7 @@ def _declare(lib) -> None:
         "wc_step_kernel_count": (C.c_uint32, []),
         "wc_step_kernel_name": (C.c_char_p, [C.c_uint32]),
         "wc_fluid_time_steps": (S, [P, C.c_float, C.c_uint32, C.c_int, P, P]),
+        "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_set_device": (S, [C.c_int]),
         "wc_device_count": (C.c_int, []),
         "wc_alloc_host": (S, [C.c_size_t, C.POINTER(P)]),
