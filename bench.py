@@ -365,19 +365,68 @@ def run_ours(args):
     return 0
 
 
+def run_batch(args):
+    """The 512-scene batched workload (4,096-65,536 particles per scene, log-uniform, seed 0):
+    autotuned, then timed like the single-scene step."""
+    from watercube_gb300 import _abi
+    from watercube_gb300.batch import Batch, batch_specs
+
+    _abi.check(_abi.lib().wc_set_device(0), "select device")
+    specs = batch_specs(512, 4096, 65536, seed=0)
+    dt = 1e-3
+    b = Batch.from_specs(specs)
+    n = b.num_particles
+    t0 = time.perf_counter()
+    tuning = b.tune(dt)
+    tune_s = time.perf_counter() - t0
+    b.step(dt, max(args.warmup, 3))
+    with Clocks(0) as clocks:
+        ms = b.time_steps(dt, args.steps, flush_l2=True)
+    total_ms = float(ms.sum())
+    d = b.diagnostics()
+    line = {
+        "metric": "particle-steps/s, 512 batched scenes (plain SPH step)",
+        "value": n * args.steps / (total_ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "512 scenes, 4,096-65,536 particles each (log-uniform), dt=1e-3", "particles": n,
+                   "l2": "flushed before every timed step (read of 2x L2), outside the timed span"},
+        "tuning": {"density_blocks_per_sm": tuning.density_blocks_per_sm,
+                   "force_blocks_per_sm": tuning.force_blocks_per_sm,
+                   "stream_blocks_per_sm": tuning.stream_blocks_per_sm, "cell_factor": tuning.cell_factor,
+                   "trials": tuning.trials, "tune_seconds": tune_s},
+        "gpu_launches": 6 * args.steps,
+        "clocks": clocks.summary(),
+        "mass_total": float(d[:, 0].sum()),
+    }
+    b.close()
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="dam1m")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512"], default="dam1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch512":
+        return run_batch(args)
     return run_ours(args)
 
 

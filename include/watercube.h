@@ -242,6 +242,72 @@ WC_API const char* wc_step_kernel_name(uint32_t index);
 WC_API wc_status wc_fluid_time_steps(wc_fluid* f, float dt, uint32_t nsteps, int flush_l2, float* step_ms,
                                      float* kernel_ms);
 
+/* ---- batches of independent scenes ---------------------------------------------------- */
+/*
+ * No counterpart in the reference (which simulates one scene). Hundreds of independent scenes
+ * with their own particle counts, kernel radius, grid and constants advance together: one
+ * global cell sort and one launch per stage for all scenes, replayed as one CUDA graph. Scene s
+ * keeps its particles in slots [offset[s], offset[s+1]) of the concatenated buffers.
+ */
+typedef struct wc_batch wc_batch;
+
+/* A scene of the batched workload: a fluid block of num_particles on a cubic lattice of spacing
+   s = (V_block / num_particles)^(1/3), h = 2 s, m = rest_density s^3, velocities N(0, sigma). */
+typedef struct wc_scene_spec {
+    uint32_t num_particles;
+    float block_min[3];
+    float block_max[3];
+    float stiffness;
+    float velocity_sigma;
+    uint64_t seed;
+} wc_scene_spec;
+
+/* The 512-scene workload's scene draw: counts log-uniform in [n_min, n_max], block sides
+   uniform in [0.2, 0.7] standing on the floor at a uniform x/z offset, stiffness uniform in
+   [2, 6], velocity sigma 0.5; all from splitmix64(seed). */
+WC_API wc_status wc_generate_batch_specs(uint64_t seed, uint32_t num_scenes, uint32_t n_min, uint32_t n_max,
+                                         wc_scene_spec* out);
+/* Finalized parameters of a scene: the dam-break preset's constants with the spec's h, m, k. */
+WC_API wc_status wc_scene_params(const wc_scene_spec* spec, wc_params* out);
+/* The scene's initial particles (num_particles entries). */
+WC_API wc_status wc_generate_scene(const wc_scene_spec* spec, const wc_params* p, wc_particle* out);
+
+WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, wc_batch** out);
+/* Upload all scenes' initial particles, concatenated in scene order (total entries). */
+WC_API wc_status wc_batch_setup(wc_batch* b, const wc_particle* initial, uint64_t total);
+WC_API wc_status wc_batch_step(wc_batch* b, float dt, uint32_t nsteps);
+WC_API wc_status wc_batch_get_particles(wc_batch* b, wc_particle* out, uint64_t total);
+WC_API wc_status wc_batch_set_particles(wc_batch* b, const wc_particle* in, uint64_t total);
+/* offsets[num_scenes + 1]: scene s owns slots [offsets[s], offsets[s+1]). */
+WC_API wc_status wc_batch_scene_offsets(const wc_batch* b, uint64_t* offsets);
+WC_API uint32_t wc_batch_num_scenes(const wc_batch* b);
+WC_API uint64_t wc_batch_num_particles(const wc_batch* b);
+/* Per-scene FP64 reductions on the device: out[6 s + 0..5] = mass, momentum x/y/z, kinetic
+   energy, potential energy (-m g.x summed). */
+WC_API wc_status wc_batch_diagnostics(wc_batch* b, double* out);
+WC_API wc_status wc_batch_time_steps(wc_batch* b, float dt, uint32_t nsteps, int flush_l2, float* step_ms);
+WC_API wc_status wc_batch_device_buffers(wc_batch* b, wc_device_buffers* out);
+WC_API void wc_batch_destroy(wc_batch* b);
+
+/* Launch geometry the autotuner picks: resident blocks per SM of the two neighbour passes and
+   of the per-particle kernels, and the cell edge as a multiple of each scene's h. */
+typedef struct wc_tuning {
+    uint32_t density_blocks_per_sm;
+    uint32_t force_blocks_per_sm;
+    uint32_t stream_blocks_per_sm;
+    float cell_factor;
+    float step_ms; /* best measured step time */
+    uint32_t trials;
+} wc_tuning;
+
+/* Time graph replays of candidate geometries (the state is saved before and restored after,
+   so the simulation does not advance) and keep the fastest; results are cached per
+   (particle count, particles per cell) for the process, and in the file named by
+   $WC_TUNE_CACHE when set. */
+WC_API wc_status wc_batch_tune(wc_batch* b, float dt, wc_tuning* out);
+WC_API wc_status wc_batch_set_tuning(wc_batch* b, const wc_tuning* t);
+WC_API wc_status wc_batch_get_tuning(const wc_batch* b, wc_tuning* out);
+
 /* ---- cell sort without allocation ------------------------------------------------------ */
 
 #define WC_NOALLOC_MAX_PARTICLES (1u << 18) /* 262,144 */

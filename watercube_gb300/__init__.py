@@ -10,3 +10,4 @@ from .fluid import (  # noqa: F401
     generate_reference_lattice,
     reference_params,
 )
+from .batch import Batch, batch_specs, scene_params, scene_particles, shard_scenes  # noqa: F401,E402

@@ -114,6 +114,28 @@ class DeviceBuffers(C.Structure):
     ]
 
 
+class SceneSpec(C.Structure):
+    _fields_ = [
+        ("num_particles", C.c_uint32),
+        ("block_min", C.c_float * 3),
+        ("block_max", C.c_float * 3),
+        ("stiffness", C.c_float),
+        ("velocity_sigma", C.c_float),
+        ("seed", C.c_uint64),
+    ]
+
+
+class Tuning(C.Structure):
+    _fields_ = [
+        ("density_blocks_per_sm", C.c_uint32),
+        ("force_blocks_per_sm", C.c_uint32),
+        ("stream_blocks_per_sm", C.c_uint32),
+        ("cell_factor", C.c_float),
+        ("step_ms", C.c_float),
+        ("trials", C.c_uint32),
+    ]
+
+
 # numpy view of `struct wc_particle` (the reference's std430 Particle, 32 bytes)
 PARTICLE_DTYPE = np.dtype(
     [("position", np.float32, (3,)), ("density", np.float32), ("velocity", np.float32, (3,)), ("pressure", np.float32)]
@@ -158,6 +180,24 @@ def _declare(lib) -> None:
         "wc_step_kernel_count": (C.c_uint32, []),
         "wc_step_kernel_name": (C.c_char_p, [C.c_uint32]),
         "wc_fluid_time_steps": (S, [P, C.c_float, C.c_uint32, C.c_int, P, P]),
+        "wc_generate_batch_specs": (S, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(SceneSpec)]),
+        "wc_scene_params": (S, [C.POINTER(SceneSpec), pp]),
+        "wc_generate_scene": (S, [C.POINTER(SceneSpec), pp, P]),
+        "wc_batch_create": (S, [pp, C.c_uint32, C.POINTER(P)]),
+        "wc_batch_setup": (S, [P, P, C.c_uint64]),
+        "wc_batch_step": (S, [P, C.c_float, C.c_uint32]),
+        "wc_batch_get_particles": (S, [P, P, C.c_uint64]),
+        "wc_batch_set_particles": (S, [P, P, C.c_uint64]),
+        "wc_batch_scene_offsets": (S, [P, C.POINTER(C.c_uint64)]),
+        "wc_batch_num_scenes": (C.c_uint32, [P]),
+        "wc_batch_num_particles": (C.c_uint64, [P]),
+        "wc_batch_diagnostics": (S, [P, C.POINTER(C.c_double)]),
+        "wc_batch_time_steps": (S, [P, C.c_float, C.c_uint32, C.c_int, P]),
+        "wc_batch_device_buffers": (S, [P, C.POINTER(DeviceBuffers)]),
+        "wc_batch_destroy": (None, [P]),
+        "wc_batch_tune": (S, [P, C.c_float, C.POINTER(Tuning)]),
+        "wc_batch_set_tuning": (S, [P, C.POINTER(Tuning)]),
+        "wc_batch_get_tuning": (S, [P, C.POINTER(Tuning)]),
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_set_device": (S, [C.c_int]),
         "wc_device_count": (C.c_int, []),

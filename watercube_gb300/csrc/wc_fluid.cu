@@ -18,30 +18,6 @@ constexpr uint32_t NUM_STEP_KERNELS = 6;
 const char* const STEP_KERNEL_NAMES[NUM_STEP_KERNELS] = {"bin_count", "scan_cells",     "scatter_cells",
                                                          "rank_gather", "density", "force_integrate"};
 
-// Host copies of the force kernel's arguments, in declaration order, so that the captured
-// graph's force node can be re-parameterised (dt, gravity, mouse ray) without re-capture.
-struct ForceArgs {
-    SceneConsts sc;
-    StepInputs in;
-    uint32_t n;
-    const float4* pos_b;
-    const float4* vel_b;
-    const uint32_t* ids_b;
-    float4* pos_a;
-    float4* vel_a;
-    uint32_t* ids_a;
-    const uint32_t* start;
-    const uint32_t* cell_list;
-    const uint32_t* num_nonempty;
-    const uint32_t* hits;
-    void* ptrs[13];
-    void bind() {
-        void* p[13] = {&sc,    &in,    &n,     &pos_b, &vel_b,     &ids_b,        &pos_a,
-                       &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits};
-        std::memcpy(ptrs, p, sizeof p);
-    }
-};
-
 bool same_inputs(const StepInputs& a, const StepInputs& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
 
 }  // namespace
@@ -61,7 +37,7 @@ struct wc_fluid {
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t force_node = nullptr;
     cudaKernelNodeParams force_params{};
-    ForceArgs fargs{};
+    ForceKernelArgs fargs{};
     StepInputs graph_in{};
     // host-copy staging (AoS, 32 bytes per particle) and error word
     float4* staging = nullptr;
@@ -198,10 +174,12 @@ wc_status capture_graph(wc_fluid* f, const StepInputs& in) {
         }
     }
     if (!f->force_node) return fail(WC_ERR_CUDA, "step graph has no force node");
-    ForceArgs& a = f->fargs;
+    ForceKernelArgs& a = f->fargs;
     a.sc = f->sc;
+    a.bt = BatchTables{};
     a.in = in;
     a.n = f->d.n;
+    a.num_cells = f->d.num_cells;
     a.pos_b = f->d.pos_b;
     a.vel_b = f->d.vel_b;
     a.ids_b = f->d.ids_b;

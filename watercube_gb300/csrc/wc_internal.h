@@ -28,6 +28,28 @@ struct SceneConsts {
     uint32_t eos, flags;
 };
 
+// Scene tables of a batch of independent scenes in one set of buffers (device memory). Scene s
+// owns particle slots [poff[s], poff[s+1]) and cell keys [coff[s], coff[s] + R_s^3); one global
+// counting sort over all keys therefore keeps every scene inside its own slot range.
+constexpr uint32_t MAX_SCENES = 1024;
+struct BatchTables {
+    const SceneConsts* scenes;  // [num_scenes]
+    const uint32_t* poff;       // [num_scenes + 1]
+    const uint32_t* coff;       // [num_scenes + 1]
+    uint32_t num_scenes;
+};
+
+// Largest s in [0, count) with offs[s] <= key, for ascending offs with offs[0] <= key.
+__device__ __forceinline__ uint32_t find_scene(const uint32_t* offs, uint32_t count, uint32_t key) {
+    uint32_t lo = 0, hi = count;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= key) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // Per-step inputs that may change between steps without re-recording the step graph.
 struct StepInputs {
     float dt;
@@ -93,8 +115,44 @@ void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, 
 void launch_soa_to_aos(const float4* pos, const float4* vel, float4* aos, uint32_t n, cudaStream_t s);
 void launch_l2_flush(const float4* buf, size_t n4, float* sink, cudaStream_t s);
 
+// The same stages over a batch of scenes (wc_batch.cu): keys carry the scene's cell offset and
+// every cell takes its scene's constants.
+void launch_bin_count_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s);
+void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s);
+void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
+                          cudaStream_t s);
+
+// Host copies of the force kernel's arguments, in declaration order, so that a captured step
+// graph's force node can be re-parameterised (dt, gravity, mouse ray) without re-capture.
+struct ForceKernelArgs {
+    SceneConsts sc;
+    BatchTables bt;
+    StepInputs in;
+    uint32_t n;
+    uint32_t num_cells;
+    const float4* pos_b;
+    const float4* vel_b;
+    const uint32_t* ids_b;
+    float4* pos_a;
+    float4* vel_a;
+    uint32_t* ids_a;
+    const uint32_t* start;
+    const uint32_t* cell_list;
+    const uint32_t* num_nonempty;
+    const uint32_t* hits;
+    void* ptrs[15];
+    void bind() {
+        void* p[15] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b,
+                       &pos_a, &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits};
+        for (int i = 0; i < 15; ++i) ptrs[i] = p[i];
+    }
+};
+
 // The kernel entry points the force node of a captured graph is recognised by.
 const void* force_kernel_symbol(uint32_t flags);
+const void* force_kernel_batched_symbol();
+// Resident blocks per SM of the two neighbour passes (single-scene or batched variant).
+void sph_occupancy(bool batched, int* density_blocks, int* force_blocks);
 
 SceneConsts make_scene_consts(const wc_params& p);
 StepInputs make_step_inputs(const wc_params& p, float dt);

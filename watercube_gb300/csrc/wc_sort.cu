@@ -55,12 +55,30 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned 
 
 // One thread per particle (grid-stride, block-uniform trip count so that every lane of a warp
 // reaches the match/vote instructions together).
+// BATCHED: particle slot i belongs to the scene whose slot range holds it; its key is that
+// scene's cell offset plus the key in the scene's own grid.
+template <bool BATCHED>
 __global__ void __launch_bounds__(256) bin_count_kernel(const float4* __restrict__ pos, uint32_t n, float bin,
-                                                        int32_t R, uint32_t* __restrict__ keys,
+                                                        int32_t R, const BatchTables bt, uint32_t* __restrict__ keys,
                                                         uint32_t* __restrict__ ranks, uint32_t* __restrict__ counts,
                                                         unsigned long long* __restrict__ scan_desc,
                                                         uint32_t* __restrict__ scan_tile_counter, uint32_t num_tiles,
                                                         uint32_t* __restrict__ err) {
+    __shared__ uint32_t s_poff[BATCHED ? MAX_SCENES + 1 : 1];
+    __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
+    __shared__ float s_bin[BATCHED ? MAX_SCENES : 1];
+    __shared__ int32_t s_R[BATCHED ? MAX_SCENES : 1];
+    if (BATCHED) {
+        for (uint32_t t = threadIdx.x; t <= bt.num_scenes; t += blockDim.x) {
+            s_poff[t] = bt.poff[t];
+            s_coff[t] = bt.coff[t];
+            if (t < bt.num_scenes) {
+                s_bin[t] = bt.scenes[t].bin;
+                s_R[t] = bt.scenes[t].R;
+            }
+        }
+        __syncthreads();
+    }
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
     // Reset the look-back state of the scan that follows this kernel on the stream.
     for (uint32_t t = gid; t < num_tiles; t += gridDim.x * blockDim.x) scan_desc[t] = 0ull;
@@ -75,7 +93,12 @@ __global__ void __launch_bounds__(256) bin_count_kernel(const float4* __restrict
         if (valid) {
             const float4 p = pos[i];
             if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(err, DEVERR_NONFINITE);
-            key = cell_key(p, bin, R);
+            if (BATCHED) {
+                const uint32_t sc = find_scene(s_poff, bt.num_scenes, i);
+                key = s_coff[sc] + cell_key(p, s_bin[sc], s_R[sc]);
+            } else {
+                key = cell_key(p, bin, R);
+            }
         }
         const unsigned vmask = __ballot_sync(FULL, valid);
         if (valid) {
@@ -270,8 +293,16 @@ void launch_bin_count(const DevBuffers& d, const SceneConsts& sc, const LaunchDi
     int grid = grid_for(d.n, ld.grid_stream);
     const int need = (int)((d.num_tiles + 255u) / 256u);
     if (grid < need) grid = need;
-    bin_count_kernel<<<grid, 256, 0, s>>>(d.pos_a, d.n, sc.bin, sc.R, d.keys, d.ranks, d.counts, d.scan_desc,
-                                          d.scan_tile_counter, d.num_tiles, d.err);
+    bin_count_kernel<false><<<grid, 256, 0, s>>>(d.pos_a, d.n, sc.bin, sc.R, BatchTables{}, d.keys, d.ranks, d.counts,
+                                                 d.scan_desc, d.scan_tile_counter, d.num_tiles, d.err);
+}
+
+void launch_bin_count_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
+    int grid = grid_for(d.n, ld.grid_stream);
+    const int need = (int)((d.num_tiles + 255u) / 256u);
+    if (grid < need) grid = need;
+    bin_count_kernel<true><<<grid, 256, 0, s>>>(d.pos_a, d.n, 0.f, 0, bt, d.keys, d.ranks, d.counts, d.scan_desc,
+                                                d.scan_tile_counter, d.num_tiles, d.err);
 }
 
 void launch_scan_cells(const DevBuffers& d, cudaStream_t s) {

@@ -255,7 +255,11 @@ __device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, 
 
 // ---- density --------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneConsts sc, const uint32_t n,
+// BATCHED: cells belong to several scenes (BatchTables); each cell takes its scene's constants
+// and indexes the scene's slice of the cell table.
+template <bool BATCHED>
+__global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneConsts sc0, const BatchTables bt,
+                                                                 const uint32_t n, const uint32_t num_cells,
                                                                  const float4* __restrict__ pos_in,
                                                                  float* rho_out,  // aliases pos_in[].w
                                                                  float* p_out,    // aliases vel[].w
@@ -265,16 +269,31 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
                                                                  uint32_t* __restrict__ ncount,
                                                                  uint32_t* __restrict__ hits) {
     __shared__ __align__(16) float s_stage[WARPS][3][STAGE_CAP];
+    __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
+    if (BATCHED) {
+        for (uint32_t t = threadIdx.x; t <= bt.num_scenes; t += blockDim.x) s_coff[t] = bt.coff[t];
+        __syncthreads();
+    }
     const uint32_t lane = threadIdx.x & 31u;
     float* sx = s_stage[threadIdx.x >> 5][0];
     float* sy = s_stage[threadIdx.x >> 5][1];
     float* sz = s_stage[threadIdx.x >> 5][2];
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t M = min(*num_nonempty, (uint32_t)sc.R * (uint32_t)sc.R * (uint32_t)sc.R);
-    const f2 cull2 = pk(sc.cull, sc.cull);
+    const uint32_t M = min(*num_nonempty, num_cells);
     for (uint32_t m = warp; m < M; m += nwarps) {
-        const CellRows cr = cell_rows(start, n, sc.R, __ldg(cell_list + m), lane);
+        const uint32_t cg = __ldg(cell_list + m);
+        SceneConsts sc;
+        uint32_t coff = 0;
+        if (BATCHED) {
+            const uint32_t s = find_scene(s_coff, bt.num_scenes, cg);
+            sc = bt.scenes[s];
+            coff = s_coff[s];
+        } else {
+            sc = sc0;
+        }
+        const f2 cull2 = pk(sc.cull, sc.cull);
+        const CellRows cr = cell_rows(start + coff, n, sc.R, cg - coff, lane);
         const uint32_t pad = stage_padding(max_slices(cr.cend - cr.cbeg));
         if (cr.total + pad <= (uint32_t)STAGE_CAP) {
             // Stage: the concatenated candidate list as x/y/z arrays, then `pad` far-away
@@ -462,8 +481,11 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     if (ids_a) ids_a[ti] = ids_b[ti];
 }
 
-__global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts sc, const StepInputs in,
-                                                               const uint32_t n, const float4* __restrict__ pos_b,
+template <bool BATCHED>
+__global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts sc0, const BatchTables bt,
+                                                               const StepInputs in, const uint32_t n,
+                                                               const uint32_t num_cells,
+                                                               const float4* __restrict__ pos_b,
                                                                const float4* __restrict__ vel_b,
                                                                const uint32_t* __restrict__ ids_b,
                                                                float4* __restrict__ pos_a, float4* __restrict__ vel_a,
@@ -474,14 +496,29 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts
                                                                const uint32_t* __restrict__ hits) {
     __shared__ uint32_t s_slot[WARPS][STAGE_CAP];             // candidate number -> sorted slot
     __shared__ uint32_t s_lists[WARPS][FORCE_LIST_CAP * 32];  // direct path: per-lane lists
+    __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
+    if (BATCHED) {
+        for (uint32_t t = threadIdx.x; t <= bt.num_scenes; t += blockDim.x) s_coff[t] = bt.coff[t];
+        __syncthreads();
+    }
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t* slot = s_slot[threadIdx.x >> 5];
     uint32_t* list = s_lists[threadIdx.x >> 5];
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t M = min(*num_nonempty, (uint32_t)sc.R * (uint32_t)sc.R * (uint32_t)sc.R);
+    const uint32_t M = min(*num_nonempty, num_cells);
     for (uint32_t m = warp; m < M; m += nwarps) {
-        const CellRows cr = cell_rows(start, n, sc.R, __ldg(cell_list + m), lane);
+        const uint32_t cg = __ldg(cell_list + m);
+        SceneConsts sc;
+        uint32_t coff = 0;
+        if (BATCHED) {
+            const uint32_t s = find_scene(s_coff, bt.num_scenes, cg);
+            sc = bt.scenes[s];
+            coff = s_coff[s];
+        } else {
+            sc = sc0;
+        }
+        const CellRows cr = cell_rows(start + coff, n, sc.R, cg - coff, lane);
         const uint32_t ncell = cr.cend - cr.cbeg;
         bool replay = false;
         if (ncell <= 32u && hits != nullptr) {
@@ -589,31 +626,59 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts
 
 }  // namespace
 
+void sph_occupancy(bool batched, int* density_blocks, int* force_blocks) {
+    int bd = 0, bf = 0;
+    if (batched) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<true>, SPH_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<true>, SPH_THREADS, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<false>, SPH_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<false>, SPH_THREADS, 0);
+    }
+    *density_blocks = bd > 0 ? bd : 1;
+    *force_blocks = bf > 0 ? bf : 1;
+}
+
 LaunchDims compute_launch_dims(int device) {
     LaunchDims ld;
     cudaDeviceGetAttribute(&ld.sms, cudaDevAttrMultiProcessorCount, device);
     if (ld.sms <= 0) ld.sms = 1;
-    int bd = 0, bf = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel, SPH_THREADS, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel, SPH_THREADS, 0);
-    ld.grid_density = ld.sms * (bd > 0 ? bd : 1);
-    ld.grid_force = ld.sms * (bf > 0 ? bf : 1);
+    int bd = 1, bf = 1;
+    sph_occupancy(false, &bd, &bf);
+    ld.grid_density = ld.sms * bd;
+    ld.grid_force = ld.sms * bf;
     ld.grid_stream = ld.sms * 8;
     return ld;
 }
 
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s) {
-    density_kernel<<<ld.grid_density, SPH_THREADS, 0, s>>>(
-        sc, d.n, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3, reinterpret_cast<float*>(d.vel_b) + 3, d.start,
-        d.cell_list, d.num_nonempty, (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr, d.hits);
+    density_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
+        sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
+        reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty,
+        (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr, d.hits);
 }
 
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s) {
-    force_kernel<<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, in, d.n, d.pos_b, d.vel_b, d.ids_b, d.pos_a, d.vel_a,
-                                                       d.ids_a, d.start, d.cell_list, d.num_nonempty, d.hits);
+    force_kernel<false><<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, BatchTables{}, in, d.n, d.num_cells, d.pos_b,
+                                                              d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
+                                                              d.cell_list, d.num_nonempty, d.hits);
 }
 
-const void* force_kernel_symbol(uint32_t) { return reinterpret_cast<const void*>(&force_kernel); }
+void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
+    density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
+        SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
+        reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits);
+}
+
+void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
+                          cudaStream_t s) {
+    force_kernel<true><<<ld.grid_force, SPH_THREADS, 0, s>>>(SceneConsts{}, bt, in, d.n, d.num_cells, d.pos_b,
+                                                             d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
+                                                             d.cell_list, d.num_nonempty, d.hits);
+}
+
+const void* force_kernel_symbol(uint32_t) { return reinterpret_cast<const void*>(&force_kernel<false>); }
+const void* force_kernel_batched_symbol() { return reinterpret_cast<const void*>(&force_kernel<true>); }
 
 }  // namespace wc
