@@ -308,6 +308,42 @@ WC_API wc_status wc_batch_tune(wc_batch* b, float dt, wc_tuning* out);
 WC_API wc_status wc_batch_set_tuning(wc_batch* b, const wc_tuning* t);
 WC_API wc_status wc_batch_get_tuning(const wc_batch* b, wc_tuning* out);
 
+/* ---- learned surrogate: network operations ---------------------------------------------- */
+/*
+ * No counterpart in the reference. Building blocks of the message-passing surrogate; all
+ * pointers are device memory; work is enqueued on `stream`; device-side failures (a bounded
+ * tensor-core wait that ran out) are OR-ed into *d_err (WC_DEVERR_* bits) when d_err is set.
+ */
+#define WC_DEVERR_MMA_TIMEOUT 4u
+
+/* C = A . B (+ bias) (+ add1[add1_idx[row]] + add2[add2_idx[row]]) (ReLU) on the tensor cores
+   (BF16 operands, FP32 accumulation), 128 x 128 output tiles. */
+typedef struct wc_gemm_desc {
+    uint32_t m, n, k;      /* k a multiple of 8 */
+    uint32_t k_chunk;      /* K range per split (multiple of 64; >= k for no split) */
+    const void* a;         /* bf16 */
+    const void* a2;        /* bf16 second source for A columns >= k_split, or NULL */
+    const uint32_t* a_rows;/* A row gather, or NULL */
+    uint32_t lda, lda2, k_split;
+    int a_transposed;      /* 0: A row-major [m x k]; 1: A[i][kk] = a[kk * lda + i] */
+    const void* b;         /* bf16 */
+    uint32_t ldb;
+    int b_rowmajor;        /* 0: b holds B^T [n x k] row-major; 1: b holds B [k x n] row-major */
+    const float* bias;     /* [n] or NULL */
+    const void* add1;      /* bf16 rows added in the epilogue, or NULL */
+    const uint32_t* add1_idx;
+    const void* add2;
+    const uint32_t* add2_idx;
+    uint32_t ld_add;
+    int relu;
+    float* c_f32;          /* fp32 output (split s at c_f32 + s * split_stride), or NULL */
+    void* c_bf16;          /* bf16 output, or NULL */
+    uint32_t ldc;
+    size_t split_stride;
+} wc_gemm_desc;
+
+WC_API wc_status wc_nn_gemm(const wc_gemm_desc* g, uint32_t* d_err, void* stream);
+
 /* ---- cell sort without allocation ------------------------------------------------------ */
 
 #define WC_NOALLOC_MAX_PARTICLES (1u << 18) /* 262,144 */

@@ -136,6 +136,18 @@ class Tuning(C.Structure):
     ]
 
 
+class GemmDesc(C.Structure):
+    _fields_ = [
+        ("m", C.c_uint32), ("n", C.c_uint32), ("k", C.c_uint32), ("k_chunk", C.c_uint32),
+        ("a", C.c_void_p), ("a2", C.c_void_p), ("a_rows", C.c_void_p),
+        ("lda", C.c_uint32), ("lda2", C.c_uint32), ("k_split", C.c_uint32), ("a_transposed", C.c_int),
+        ("b", C.c_void_p), ("ldb", C.c_uint32), ("b_rowmajor", C.c_int),
+        ("bias", C.c_void_p), ("add1", C.c_void_p), ("add1_idx", C.c_void_p), ("add2", C.c_void_p),
+        ("add2_idx", C.c_void_p), ("ld_add", C.c_uint32), ("relu", C.c_int),
+        ("c_f32", C.c_void_p), ("c_bf16", C.c_void_p), ("ldc", C.c_uint32), ("split_stride", C.c_size_t),
+    ]
+
+
 # numpy view of `struct wc_particle` (the reference's std430 Particle, 32 bytes)
 PARTICLE_DTYPE = np.dtype(
     [("position", np.float32, (3,)), ("density", np.float32), ("velocity", np.float32, (3,)), ("pressure", np.float32)]
@@ -198,6 +210,7 @@ def _declare(lib) -> None:
         "wc_batch_tune": (S, [P, C.c_float, C.POINTER(Tuning)]),
         "wc_batch_set_tuning": (S, [P, C.POINTER(Tuning)]),
         "wc_batch_get_tuning": (S, [P, C.POINTER(Tuning)]),
+        "wc_nn_gemm": (S, [C.POINTER(GemmDesc), P, P]),
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_set_device": (S, [C.c_int]),
         "wc_device_count": (C.c_int, []),

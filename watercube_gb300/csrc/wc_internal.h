@@ -12,7 +12,8 @@ namespace wc {
 // Device error bits (OR-ed into DevBuffers::err by kernels; read at synchronisation points).
 enum : uint32_t {
     DEVERR_NONFINITE = 1u << 0,    // a non-finite position was binned
-    DEVERR_SCAN_TIMEOUT = 1u << 1  // a scan tile gave up waiting on its predecessor
+    DEVERR_SCAN_TIMEOUT = 1u << 1,  // a scan tile gave up waiting on its predecessor
+    DEVERR_MMA_TIMEOUT = 1u << 2    // a tensor-core GEMM gave up waiting on its MMAs
 };
 
 // Constants of one scene, by value in kernel parameters (single scene) or in a device table

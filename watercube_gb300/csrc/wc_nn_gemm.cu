@@ -1,0 +1,342 @@
+// wc_nn_gemm.cu — BF16 tensor-core GEMM for the learned surrogate (sm_103a tcgen05 + TMEM).
+//
+//   C[m, n] = sum_k A[m, k] * B[k, n]        (BF16 operands, FP32 accumulation in TMEM)
+//
+// One CTA (4 warps) computes a 128 x 128 tile of C. Per 64-deep slice of K, all threads stage
+// the A and B tiles into shared memory in the canonical no-swizzle K-major layout of the
+// tensor-core descriptors (8-row x 16-byte core matrices; the next core matrix along K is 128 B
+// away, the next 8-row group 1,024 B away), fence them into the async proxy, and one thread
+// issues four tcgen05.mma (K = 16 each) into a 128-column FP32 accumulator in tensor memory and
+// commits them to an mbarrier. The epilogue reads the accumulator with tcgen05.ld (warp w owns
+// rows 32w..32w+31, one row per thread) and applies bias, row gathers, ReLU and the store.
+//
+// Operand sources (staging policies):
+//   A row-major [m x k] (lda), optionally with a row index (gather) and a second source for
+//     the columns at and after k_split (concatenation [X | Y]); or A transposed: A[i][kk] =
+//     a[kk * lda + i] (the weight-gradient GEMM X^T dY).
+//   B as B^T row-major [n x k] (ldb) (a weight matrix stored output-major), or B row-major
+//     [k x n] (the upstream gradient dY in X^T dY, and W in dY W^T).
+// Every wait on the mbarrier is bounded; a wait that runs out sets an error flag, and the
+// kernel still releases its tensor memory before it returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "wc_internal.h"
+#include "wc_nn.h"
+#include "wc_util.h"
+
+namespace wc {
+namespace nn {
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int THREADS = 128;
+constexpr uint32_t TMEM_COLS = 128;
+constexpr uint32_t WAIT_LIMIT = 1u << 22;
+
+// Instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and
+// B (bits 7-9 = 1, bits 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+struct __align__(1024) Tiles {
+    __nv_bfloat16 a[BM * BK];  // 16 KB
+    __nv_bfloat16 b[BN * BK];  // 16 KB
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start >> 4, LBO = 128 B (next core matrix along K),
+// SBO = 1024 B (next 8-row group), version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)(128u >> 4) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Byte offset of element (r, k) of a 128 x 64 tile in the core-matrix layout.
+__device__ __forceinline__ uint32_t tile_off(uint32_t r, uint32_t k) {
+    return (((r >> 3) * 8u + (k >> 3)) << 7) + ((r & 7u) << 4) + ((k & 7u) << 1);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Stage a 128 x 64 slice of an operand: rows [row0, row0 + 128) of the logical matrix, columns
+// [k0, k0 + 64). T = transposed source (logical (r, k) = src[k * ld + r]).
+struct OperandSrc {
+    const __nv_bfloat16* p;   // primary source
+    const __nv_bfloat16* p2;  // second source for columns >= k_split (row-major only), or null
+    const uint32_t* rows;     // row gather (row-major only), or null
+    uint32_t ld, ld2, k_split;
+    uint32_t nrows, ncols;    // logical extent
+    int transposed;
+};
+
+__device__ __forceinline__ void stage(const OperandSrc& s, __nv_bfloat16* tile, uint32_t row0, uint32_t k0) {
+    unsigned char* base = reinterpret_cast<unsigned char*>(tile);
+    if (!s.transposed) {
+        // 1,024 chunks of 8 elements (16 B); chunk id -> (row r, k-group g).
+        for (uint32_t id = threadIdx.x; id < (uint32_t)(BM * BK / 8); id += THREADS) {
+            const uint32_t r = id >> 3, g = id & 7u;
+            const uint32_t row = row0 + r, col = k0 + 8u * g;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (row < s.nrows && col < s.ncols) {
+                const uint32_t src_row = s.rows ? __ldg(s.rows + row) : row;
+                const __nv_bfloat16* src;
+                if (s.p2 && col >= s.k_split)
+                    src = s.p2 + (size_t)src_row * s.ld2 + (col - s.k_split);
+                else
+                    src = s.p + (size_t)src_row * s.ld + col;
+                v = __ldg(reinterpret_cast<const uint4*>(src));
+            }
+            *reinterpret_cast<uint4*>(base + tile_off(r, 8u * g)) = v;
+        }
+    } else {
+        // 1,024 chunks of 8 consecutive logical rows at one k: src[k * ld + r .. r + 7].
+        for (uint32_t id = threadIdx.x; id < (uint32_t)(BM * BK / 8); id += THREADS) {
+            const uint32_t k = id >> 4, rg = id & 15u;
+            const uint32_t kk = k0 + k, r = row0 + 8u * rg;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (kk < s.ncols && r < s.nrows) v = __ldg(reinterpret_cast<const uint4*>(s.p + (size_t)kk * s.ld + r));
+            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j)
+                *reinterpret_cast<__nv_bfloat16*>(base + tile_off(8u * rg + j, k)) = e[j];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_t* err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    Tiles& t = *reinterpret_cast<Tiles*>(smem_raw);
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_failed;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const uint32_t kz = blockIdx.z;  // split of the K range (weight gradients)
+    const uint32_t k_begin = kz * g.k_chunk;
+    const uint32_t k_end = min(g.k, k_begin + g.k_chunk);
+
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_failed = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    OperandSrc A{g.a, g.a2, g.a_rows, g.lda, g.lda2, g.k_split, g.m, g.k, g.a_transposed};
+    // B is staged as B^T (rows = output columns n, columns = k).
+    OperandSrc B{g.b, nullptr, nullptr, g.ldb, 0u, 0u, g.n, g.k, g.b_rowmajor};
+
+    const uint32_t a_base = smem_addr(t.a), b_base = smem_addr(t.b);
+    uint32_t phase = 0;
+    bool ok = true;
+    uint32_t issued = 0;
+    for (uint32_t k0 = k_begin; k0 < k_end; k0 += BK) {
+        if (issued) {
+            // The previous slice's MMAs must finish reading the tiles before they are rewritten.
+            if (!mbar_wait(smem_addr(&mbar), phase)) ok = false;
+            phase ^= 1u;
+        }
+        stage(A, t.a, m0, k0);
+        stage(B, t.b, n0, k0);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (uint32_t j = 0; j < BK / 16; ++j) {
+                const uint64_t ad = smem_desc(a_base + 256u * j);
+                const uint64_t bd = smem_desc(b_base + 256u * j);
+                const uint32_t acc = (issued > 0 || j > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&mbar))
+                         : "memory");
+        }
+        ++issued;
+    }
+    if (issued) {
+        if (!mbar_wait(smem_addr(&mbar), phase)) ok = false;
+    }
+    if (!ok) atomicOr(&s_failed, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    const bool failed = s_failed != 0;
+    if (failed && threadIdx.x == 0 && err) atomicOr(err, DEVERR_MMA_TIMEOUT);
+
+    // Epilogue: thread owns row m0 + 32 warp + lane; columns in chunks of 32.
+    const uint32_t row = m0 + 32u * warp + lane;
+    const bool row_ok = row < g.m && !failed;
+    for (uint32_t c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((32u * warp) << 16) + c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+              "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (!row_ok || n0 + c0 >= g.n) continue;
+        const uint32_t ncols = min(32u, g.n - (n0 + c0));
+        float x[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) x[j] = issued ? __uint_as_float(v[j]) : 0.f;
+        const uint32_t col0 = n0 + c0;
+        if (g.bias) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if ((uint32_t)j < ncols) x[j] += __ldg(g.bias + col0 + j);
+        }
+        if (g.add1) {
+            const __nv_bfloat16* r1 = g.add1 + (size_t)__ldg(g.add1_idx + row) * g.ld_add + col0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if ((uint32_t)j < ncols) x[j] += __bfloat162float(r1[j]);
+        }
+        if (g.add2) {
+            const __nv_bfloat16* r2 = g.add2 + (size_t)__ldg(g.add2_idx + row) * g.ld_add + col0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if ((uint32_t)j < ncols) x[j] += __bfloat162float(r2[j]);
+        }
+        if (g.relu) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) x[j] = fmaxf(x[j], 0.f);
+        }
+        if (g.c_f32) {
+            float* out = g.c_f32 + (size_t)kz * g.split_stride + (size_t)row * g.ldc + col0;
+            if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
+#pragma unroll
+                for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(out + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+            } else {
+                for (uint32_t j = 0; j < ncols; ++j) out[j] = x[j];
+            }
+        }
+        if (g.c_bf16) {
+            __nv_bfloat16* out = g.c_bf16 + (size_t)row * g.ldc + col0;
+            if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) {
+                    __nv_bfloat162 q0 = __floats2bfloat162_rn(x[j], x[j + 1]);
+                    __nv_bfloat162 q1 = __floats2bfloat162_rn(x[j + 2], x[j + 3]);
+                    __nv_bfloat162 q2 = __floats2bfloat162_rn(x[j + 4], x[j + 5]);
+                    __nv_bfloat162 q3 = __floats2bfloat162_rn(x[j + 6], x[j + 7]);
+                    uint4 w;
+                    w.x = *reinterpret_cast<uint32_t*>(&q0);
+                    w.y = *reinterpret_cast<uint32_t*>(&q1);
+                    w.z = *reinterpret_cast<uint32_t*>(&q2);
+                    w.w = *reinterpret_cast<uint32_t*>(&q3);
+                    *reinterpret_cast<uint4*>(out + j) = w;
+                }
+            } else {
+                for (uint32_t j = 0; j < ncols; ++j) out[j] = __float2bfloat16_rn(x[j]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+}  // namespace
+
+// At most four CTAs per SM: 4 x 128 accumulator columns fill the SM's 512 columns of tensor
+// memory exactly, so tcgen05.alloc never has to wait for another CTA.
+size_t gemm_smem_bytes() { return 57u * 1024u; }
+
+wc_status check_gemm(const GemmArgs& g) {
+    if (g.m == 0 || g.n == 0) return WC_OK;
+    if (!g.a || !g.b || (!g.c_f32 && !g.c_bf16)) return fail(WC_ERR_INVALID_ARG, "gemm: null operand");
+    if (!g.a_transposed && (g.lda % 8 || (g.a2 && (g.lda2 % 8 || g.k_split % 8))))
+        return fail(WC_ERR_INVALID_ARG, "gemm: row-major A needs 16-byte aligned rows (lda %% 8 == 0)");
+    if (g.a_transposed && (g.lda % 8 || g.m % 8)) return fail(WC_ERR_INVALID_ARG, "gemm: transposed A needs m, lda %% 8 == 0");
+    if (!g.b_rowmajor && g.ldb % 8) return fail(WC_ERR_INVALID_ARG, "gemm: B^T rows need ldb %% 8 == 0");
+    if (g.b_rowmajor && (g.ldb % 8 || g.n % 8)) return fail(WC_ERR_INVALID_ARG, "gemm: row-major B needs n, ldb %% 8 == 0");
+    if (g.k % 8) return fail(WC_ERR_INVALID_ARG, "gemm: k must be a multiple of 8 (pad with zeros)");
+    if ((g.add1 && !g.add1_idx) || (g.add2 && !g.add2_idx)) return fail(WC_ERR_INVALID_ARG, "gemm: gather without index");
+    if (g.k_chunk == 0 || g.k_chunk % BK) return fail(WC_ERR_INVALID_ARG, "gemm: k_chunk must be a multiple of 64");
+    return WC_OK;
+}
+
+wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s) {
+    const wc_status st = check_gemm(g);
+    if (st != WC_OK || g.m == 0 || g.n == 0) return st;
+    static bool attr_done = false;
+    if (!attr_done) {
+        cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());
+        attr_done = true;
+    }
+    const dim3 grid((g.m + BM - 1) / BM, (g.n + BN - 1) / BN, (g.k + g.k_chunk - 1) / g.k_chunk);
+    gemm_kernel<<<grid, THREADS, gemm_smem_bytes(), s>>>(g, err);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(WC_ERR_CUDA, "gemm launch: %s", cudaGetErrorString(e));
+    return WC_OK;
+}
+
+}  // namespace nn
+}  // namespace wc
+
+extern "C" WC_API wc_status wc_nn_gemm(const wc_gemm_desc* d, uint32_t* d_err, void* stream) {
+    wc::clear_error();
+    if (!d) return wc::fail(WC_ERR_INVALID_ARG, "wc_nn_gemm: null descriptor");
+    wc::nn::GemmArgs g{};
+    g.m = d->m;
+    g.n = d->n;
+    g.k = d->k;
+    g.k_chunk = d->k_chunk;
+    g.a = static_cast<const __nv_bfloat16*>(d->a);
+    g.a2 = static_cast<const __nv_bfloat16*>(d->a2);
+    g.a_rows = d->a_rows;
+    g.lda = d->lda;
+    g.lda2 = d->lda2;
+    g.k_split = d->k_split;
+    g.a_transposed = d->a_transposed;
+    g.b = static_cast<const __nv_bfloat16*>(d->b);
+    g.ldb = d->ldb;
+    g.b_rowmajor = d->b_rowmajor;
+    g.bias = d->bias;
+    g.add1 = static_cast<const __nv_bfloat16*>(d->add1);
+    g.add1_idx = d->add1_idx;
+    g.add2 = static_cast<const __nv_bfloat16*>(d->add2);
+    g.add2_idx = d->add2_idx;
+    g.ld_add = d->ld_add;
+    g.relu = d->relu;
+    g.c_f32 = d->c_f32;
+    g.c_bf16 = static_cast<__nv_bfloat16*>(d->c_bf16);
+    g.ldc = d->ldc;
+    g.split_stride = d->split_stride;
+    return wc::nn::launch_gemm(g, d_err, static_cast<cudaStream_t>(stream));
+}
