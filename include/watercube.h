@@ -222,6 +222,10 @@ WC_API wc_status wc_fluid_get_device_buffers(wc_fluid* f, wc_device_buffers* out
    (WC_ERR_NUMERIC, WC_ERR_TIMEOUT). */
 WC_API wc_status wc_fluid_synchronize(wc_fluid* f);
 
+/* As wc_batch_set_recording / wc_batch_get_accelerations, for one fluid. */
+WC_API wc_status wc_fluid_set_recording(wc_fluid* f, int on);
+WC_API wc_status wc_fluid_get_accelerations(wc_fluid* f, float* out /* n x 4 */, uint32_t n);
+
 /* Steps taken since setup. */
 WC_API uint64_t wc_fluid_step_count(const wc_fluid* f);
 
@@ -287,6 +291,12 @@ WC_API uint64_t wc_batch_num_particles(const wc_batch* b);
 WC_API wc_status wc_batch_diagnostics(wc_batch* b, double* out);
 WC_API wc_status wc_batch_time_steps(wc_batch* b, float dt, uint32_t nsteps, int flush_l2, float* step_ms);
 WC_API wc_status wc_batch_device_buffers(wc_batch* b, wc_device_buffers* out);
+/* Training-data recording: when on, every step also stores each particle's SPH acceleration
+   (forces / density, before the speed clamp and wall collision), in the state buffer's order. */
+WC_API wc_status wc_batch_set_recording(wc_batch* b, int on);
+WC_API wc_status wc_batch_get_accelerations(wc_batch* b, float* out /* total x 4 */, uint64_t total);
+/* Original index (global slot at setup) of each state-buffer particle. */
+WC_API wc_status wc_batch_get_ids(wc_batch* b, uint32_t* out, uint64_t total);
 WC_API void wc_batch_destroy(wc_batch* b);
 
 /* Launch geometry the autotuner picks: resident blocks per SM of the two neighbour passes and
@@ -319,7 +329,7 @@ WC_API wc_status wc_batch_get_tuning(const wc_batch* b, wc_tuning* out);
 /* C = A . B (+ bias) (+ add1[add1_idx[row]] + add2[add2_idx[row]]) (ReLU) on the tensor cores
    (BF16 operands, FP32 accumulation), 128 x 128 output tiles. */
 typedef struct wc_gemm_desc {
-    uint32_t m, n, k;      /* k a multiple of 8 */
+    uint32_t m, n, k;      /* k a multiple of 8, unless A is transposed and B row-major */
     uint32_t k_chunk;      /* K range per split (multiple of 64; >= k for no split) */
     const void* a;         /* bf16 */
     const void* a2;        /* bf16 second source for A columns >= k_split, or NULL */
@@ -340,9 +350,78 @@ typedef struct wc_gemm_desc {
     void* c_bf16;          /* bf16 output, or NULL */
     uint32_t ldc;
     size_t split_stride;
+    int accumulate;        /* non-zero: c_f32 += result */
 } wc_gemm_desc;
 
 WC_API wc_status wc_nn_gemm(const wc_gemm_desc* g, uint32_t* d_err, void* stream);
+
+/* ---- learned surrogate: network, training and judged rollout ---------------------------- */
+/*
+ * No counterpart in the reference. A message-passing network over the radius-h graph of a
+ * fluid (latent width 128, `layers` message-passing steps) predicts each particle's SPH
+ * acceleration from its last five velocities, its wall distances and the scene's stiffness.
+ * Inputs and outputs are in the fluid's state-buffer order; the network works in the sorted
+ * order internally.
+ */
+typedef struct wc_surrogate wc_surrogate;
+
+typedef struct wc_surrogate_config {
+    uint32_t layers;      /* message-passing steps (default 8) */
+    uint64_t seed;        /* weight initialisation */
+    float velocity_scale; /* velocities are divided by this in the features (default 1) */
+    float accel_scale;    /* network outputs are multiplied by this (default 10) */
+} wc_surrogate_config;
+
+WC_API void wc_surrogate_config_default(wc_surrogate_config* c);
+WC_API wc_status wc_surrogate_create(const wc_surrogate_config* c, wc_surrogate** out);
+WC_API void wc_surrogate_destroy(wc_surrogate* s);
+/* FP32 master weights, all layers in one buffer (Adam runs over it in one launch). */
+WC_API uint64_t wc_surrogate_num_params(const wc_surrogate* s);
+WC_API wc_status wc_surrogate_get_params(wc_surrogate* s, float* host, uint64_t n);
+WC_API wc_status wc_surrogate_set_params(wc_surrogate* s, const float* host, uint64_t n);
+/* Gradients accumulated since the last wc_surrogate_adam / wc_surrogate_zero_grads. */
+WC_API wc_status wc_surrogate_get_grads(wc_surrogate* s, float* host, uint64_t n);
+WC_API wc_status wc_surrogate_zero_grads(wc_surrogate* s);
+/* Load one training sample: the fluid's current particles (positions and velocities, set
+   with wc_fluid_set_particles), the velocity history hist[5][n][4] (hist[0] = current
+   velocity, hist[k] = k steps ago) and, optionally, the target accelerations target[n][4].
+   Sorts the fluid and builds the graph and features. */
+WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, const float* hist, const float* target);
+/* Forward pass on the loaded sample; with do_backward, the gradients of the mean squared error
+   (per component, outputs scaled by 1 / accel_scale) are added to the accumulated ones. *loss
+   (may be NULL) receives that error. */
+WC_API wc_status wc_surrogate_forward_backward(wc_surrogate* s, int do_backward, double* loss);
+/* Predicted accelerations of the loaded sample, out[n][4] in state order. */
+WC_API wc_status wc_surrogate_predictions(wc_surrogate* s, float* out, uint32_t n);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) with gradients multiplied by grad_scale first;
+   clears the accumulated gradients. */
+WC_API wc_status wc_surrogate_adam(wc_surrogate* s, float lr, float grad_scale);
+
+typedef struct wc_rollout_stats {
+    uint32_t steps, sph_steps, surrogate_steps, judged, reverted;
+    uint32_t reserved;
+    double mean_density_error; /* mean over judged steps of mean_i |rho_sur_i / rho_sph_i - 1| */
+    double max_density_error;
+    double ms_device;          /* CUDA-event time of the whole rollout */
+    double ms_wall;
+    double particle_steps_per_s;
+    double diag_start[6];      /* mass, momentum x/y/z, kinetic, potential energy (FP64) */
+    double diag_end[6];
+} wc_rollout_stats;
+
+/* Rollout modes. SPH: plain solver steps (graph replays). SURROGATE: the network advances the
+   fluid. STALE: the method without the network, which reuses the last SPH acceleration for
+   the skipped steps (its first step is a plain SPH step that records one). */
+#define WC_ROLLOUT_SPH 0
+#define WC_ROLLOUT_SURROGATE 1
+#define WC_ROLLOUT_STALE 2
+
+/* Advance the fluid nsteps in `mode`. In the SURROGATE and STALE modes every K-th step is
+   judged: SPH and the candidate both advance the same state, the SPH densities of the two next
+   states are compared particle by particle, and the SPH state is kept (the step is reverted)
+   when the mean |rho_candidate / rho_SPH - 1| exceeds `tolerance`. s may be NULL for SPH. */
+WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t K,
+                                      float tolerance, int mode, wc_rollout_stats* stats);
 
 /* ---- cell sort without allocation ------------------------------------------------------ */
 

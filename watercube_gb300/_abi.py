@@ -145,7 +145,34 @@ class GemmDesc(C.Structure):
         ("bias", C.c_void_p), ("add1", C.c_void_p), ("add1_idx", C.c_void_p), ("add2", C.c_void_p),
         ("add2_idx", C.c_void_p), ("ld_add", C.c_uint32), ("relu", C.c_int),
         ("c_f32", C.c_void_p), ("c_bf16", C.c_void_p), ("ldc", C.c_uint32), ("split_stride", C.c_size_t),
+        ("accumulate", C.c_int),
     ]
+
+
+class SurrogateConfig(C.Structure):
+    _fields_ = [
+        ("layers", C.c_uint32),
+        ("seed", C.c_uint64),
+        ("velocity_scale", C.c_float),
+        ("accel_scale", C.c_float),
+    ]
+
+
+class RolloutStats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_uint32), ("sph_steps", C.c_uint32), ("surrogate_steps", C.c_uint32),
+        ("judged", C.c_uint32), ("reverted", C.c_uint32), ("reserved", C.c_uint32),
+        ("mean_density_error", C.c_double), ("max_density_error", C.c_double),
+        ("ms_device", C.c_double), ("ms_wall", C.c_double), ("particle_steps_per_s", C.c_double),
+        ("diag_start", C.c_double * 6), ("diag_end", C.c_double * 6),
+    ]
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if name.startswith("diag") else v
+        return out
 
 
 # numpy view of `struct wc_particle` (the reference's std430 Particle, 32 bytes)
@@ -206,11 +233,29 @@ def _declare(lib) -> None:
         "wc_batch_diagnostics": (S, [P, C.POINTER(C.c_double)]),
         "wc_batch_time_steps": (S, [P, C.c_float, C.c_uint32, C.c_int, P]),
         "wc_batch_device_buffers": (S, [P, C.POINTER(DeviceBuffers)]),
+        "wc_batch_set_recording": (S, [P, S]),
+        "wc_batch_get_accelerations": (S, [P, P, C.c_uint64]),
+        "wc_batch_get_ids": (S, [P, P, C.c_uint64]),
+        "wc_fluid_set_recording": (S, [P, S]),
+        "wc_fluid_get_accelerations": (S, [P, P, C.c_uint32]),
         "wc_batch_destroy": (None, [P]),
         "wc_batch_tune": (S, [P, C.c_float, C.POINTER(Tuning)]),
         "wc_batch_set_tuning": (S, [P, C.POINTER(Tuning)]),
         "wc_batch_get_tuning": (S, [P, C.POINTER(Tuning)]),
         "wc_nn_gemm": (S, [C.POINTER(GemmDesc), P, P]),
+        "wc_surrogate_config_default": (None, [C.POINTER(SurrogateConfig)]),
+        "wc_surrogate_create": (S, [C.POINTER(SurrogateConfig), C.POINTER(P)]),
+        "wc_surrogate_destroy": (None, [P]),
+        "wc_surrogate_num_params": (C.c_uint64, [P]),
+        "wc_surrogate_get_params": (S, [P, P, C.c_uint64]),
+        "wc_surrogate_set_params": (S, [P, P, C.c_uint64]),
+        "wc_surrogate_get_grads": (S, [P, P, C.c_uint64]),
+        "wc_surrogate_zero_grads": (S, [P]),
+        "wc_surrogate_sample": (S, [P, P, P, P]),
+        "wc_surrogate_forward_backward": (S, [P, S, C.POINTER(C.c_double)]),
+        "wc_surrogate_predictions": (S, [P, P, C.c_uint32]),
+        "wc_surrogate_adam": (S, [P, C.c_float, C.c_float]),
+        "wc_surrogate_rollout": (S, [P, P, C.c_float, C.c_uint32, C.c_uint32, C.c_float, S, C.POINTER(RolloutStats)]),
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_set_device": (S, [C.c_int]),
         "wc_device_count": (C.c_int, []),

@@ -152,7 +152,8 @@ void free_batch(wc_batch* b) {
     void* ptrs[] = {d.pos_a,     d.vel_a,        d.pos_b,      d.vel_b,  d.keys,         d.ranks,
                     d.unordered, d.perm,         d.counts,     d.start,  d.cell_list,    d.num_nonempty,
                     d.scan_desc, d.scan_tile_counter, d.err,   d.hits,   b->d_scenes,    b->d_poff,
-                    b->d_coff,   b->d_diag,      b->staging,   b->flush_buf, b->flush_sink};
+                    b->d_coff,   b->d_diag,      b->staging,   b->flush_buf, b->flush_sink, d.ids_a,
+                    d.ids_b,     d.accel};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->h_err) cudaFreeHost(b->h_err);
@@ -246,14 +247,15 @@ wc_status capture(wc_batch* b, const StepInputs& in) {
     a.num_cells = b->d.num_cells;
     a.pos_b = b->d.pos_b;
     a.vel_b = b->d.vel_b;
-    a.ids_b = nullptr;
+    a.ids_b = b->d.ids_b;
     a.pos_a = b->d.pos_a;
     a.vel_a = b->d.vel_a;
-    a.ids_a = nullptr;
+    a.ids_a = b->d.ids_a;
     a.start = b->d.start;
     a.cell_list = b->d.cell_list;
     a.num_nonempty = b->d.num_nonempty;
     a.hits = b->d.hits;
+    a.accel = b->d.accel;
     a.bind();
     b->graph_in = in;
     return WC_OK;
@@ -499,6 +501,8 @@ WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, w
     if (st == WC_OK) st = dalloc(&d.ranks, n);
     if (st == WC_OK) st = dalloc(&d.unordered, n);
     if (st == WC_OK) st = dalloc(&d.perm, n);
+    if (st == WC_OK) st = dalloc(&d.ids_a, n);
+    if (st == WC_OK) st = dalloc(&d.ids_b, n);
     if (st == WC_OK) st = dalloc(&d.hits, (size_t)n * MASK_WORDS);
     if (st == WC_OK) st = dalloc(&d.counts, cells);
     if (st == WC_OK) st = dalloc(&d.start, cells + 1);
@@ -561,8 +565,46 @@ WC_API wc_status wc_batch_set_particles(wc_batch* b, const wc_particle* in, uint
 
 WC_API wc_status wc_batch_setup(wc_batch* b, const wc_particle* initial, uint64_t total) {
     WC_TRY(wc_batch_set_particles(b, initial, total));
+    if (b->n) {
+        std::vector<uint32_t> iota(b->n);
+        for (uint64_t i = 0; i < b->n; ++i) iota[i] = (uint32_t)i;
+        WC_CUDA_TRY(cudaMemcpyAsync(b->d.ids_a, iota.data(), sizeof(uint32_t) * b->n, cudaMemcpyHostToDevice, b->stream));
+        WC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    }
     b->setup_done = true;
     return WC_OK;
+}
+
+WC_API wc_status wc_batch_set_recording(wc_batch* b, int on) {
+    clear_error();
+    WC_TRY(require(b, false));
+    if (on && !b->d.accel) {
+        WC_TRY(dalloc(&b->d.accel, b->n));
+        if (b->n) WC_CUDA_TRY(cudaMemsetAsync(b->d.accel, 0, sizeof(float4) * b->n, b->stream));
+    } else if (!on && b->d.accel) {
+        WC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+        cudaFree(b->d.accel);
+        b->d.accel = nullptr;
+    }
+    drop_graph(b);
+    return WC_OK;
+}
+
+WC_API wc_status wc_batch_get_accelerations(wc_batch* b, float* out, uint64_t total) {
+    clear_error();
+    WC_TRY(require(b, false));
+    if (!b->d.accel) return fail(WC_ERR_STATE, "recording is off (wc_batch_set_recording)");
+    if (total != b->n || (!out && total)) return fail(WC_ERR_INVALID_ARG, "bad acceleration buffer");
+    if (total) WC_CUDA_TRY(cudaMemcpyAsync(out, b->d.accel, sizeof(float4) * total, cudaMemcpyDeviceToHost, b->stream));
+    return read_errors(b);
+}
+
+WC_API wc_status wc_batch_get_ids(wc_batch* b, uint32_t* out, uint64_t total) {
+    clear_error();
+    WC_TRY(require(b, false));
+    if (total != b->n || (!out && total)) return fail(WC_ERR_INVALID_ARG, "bad id buffer");
+    if (total) WC_CUDA_TRY(cudaMemcpyAsync(out, b->d.ids_a, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost, b->stream));
+    return read_errors(b);
 }
 
 WC_API wc_status wc_batch_get_particles(wc_batch* b, wc_particle* out, uint64_t total) {

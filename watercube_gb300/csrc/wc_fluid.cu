@@ -69,7 +69,7 @@ void free_all(wc_fluid* f) {
     void* ptrs[] = {d.pos_a,     d.vel_a,        d.pos_b,     d.vel_b,    d.ids_a,           d.ids_b,
                     d.keys,      d.ranks,        d.unordered, d.perm,     d.counts,          d.start,
                     d.cell_list, d.num_nonempty, d.scan_desc, d.ncount,   d.scan_tile_counter, d.err,
-                    d.hits,      f->staging,     f->flush_buf, f->flush_sink};
+                    d.hits,      f->staging,     f->flush_buf, f->flush_sink, d.accel};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (f->h_err) cudaFreeHost(f->h_err);
@@ -190,6 +190,7 @@ wc_status capture_graph(wc_fluid* f, const StepInputs& in) {
     a.cell_list = f->d.cell_list;
     a.num_nonempty = f->d.num_nonempty;
     a.hits = f->d.hits;
+    a.accel = f->d.accel;
     a.bind();
     f->graph_in = in;
     return WC_OK;
@@ -233,6 +234,23 @@ wc_status require(const wc_fluid* f, bool need_setup) {
 }
 
 }  // namespace
+
+namespace wc {
+
+FluidInternals fluid_internals(wc_fluid* f) {
+    return FluidInternals{&f->d, &f->sc, &f->in, &f->params, f->stream};
+}
+
+void fluid_enqueue_sort(wc_fluid* f) { enqueue_sort(f); }
+
+wc_status fluid_graph_step(wc_fluid* f, float dt) {
+    f->in.dt = dt;
+    return launch_step(f, f->in);
+}
+
+void fluid_count_step(wc_fluid* f) { ++f->steps; }
+
+}  // namespace wc
 
 extern "C" {
 
@@ -460,6 +478,34 @@ WC_API wc_status wc_fluid_synchronize(wc_fluid* f) {
 }
 
 WC_API uint64_t wc_fluid_step_count(const wc_fluid* f) { return f ? f->steps : 0; }
+
+WC_API wc_status wc_fluid_set_recording(wc_fluid* f, int on) {
+    clear_error();
+    WC_TRY(require(f, false));
+    if (on && !f->d.accel) {
+        WC_TRY(dalloc(&f->d.accel, f->d.n));
+        if (f->d.n) WC_CUDA_TRY(cudaMemsetAsync(f->d.accel, 0, sizeof(float4) * f->d.n, f->stream));
+    } else if (!on && f->d.accel) {
+        WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
+        cudaFree(f->d.accel);
+        f->d.accel = nullptr;
+    }
+    if (f->exec) cudaGraphExecDestroy(f->exec);
+    if (f->graph) cudaGraphDestroy(f->graph);
+    f->exec = nullptr;
+    f->graph = nullptr;
+    f->force_node = nullptr;
+    return WC_OK;
+}
+
+WC_API wc_status wc_fluid_get_accelerations(wc_fluid* f, float* out, uint32_t n) {
+    clear_error();
+    WC_TRY(require(f, false));
+    if (!f->d.accel) return fail(WC_ERR_STATE, "recording is off (wc_fluid_set_recording)");
+    if (n != f->d.n || (!out && n)) return fail(WC_ERR_INVALID_ARG, "bad acceleration buffer");
+    if (n) WC_CUDA_TRY(cudaMemcpyAsync(out, f->d.accel, sizeof(float4) * n, cudaMemcpyDeviceToHost, f->stream));
+    return read_device_errors(f);
+}
 
 WC_API uint32_t wc_step_kernel_count(void) { return NUM_STEP_KERNELS; }
 

@@ -90,6 +90,7 @@ struct DevBuffers {
     uint32_t* scan_tile_counter;
     uint32_t* ncount;  // [n] or null
     uint32_t* hits;    // [n * MASK_WORDS] neighbour bit strings
+    float4* accel;     // [n] acceleration of each particle in the last force pass, or null
     uint32_t* err;
 };
 
@@ -141,11 +142,12 @@ struct ForceKernelArgs {
     const uint32_t* cell_list;
     const uint32_t* num_nonempty;
     const uint32_t* hits;
-    void* ptrs[15];
+    float4* accel;
+    void* ptrs[16];
     void bind() {
-        void* p[15] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b,
-                       &pos_a, &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits};
-        for (int i = 0; i < 15; ++i) ptrs[i] = p[i];
+        void* p[16] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b,
+                       &pos_a, &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits,  &accel};
+        for (int i = 0; i < 16; ++i) ptrs[i] = p[i];
     }
 };
 
@@ -154,6 +156,19 @@ const void* force_kernel_symbol(uint32_t flags);
 const void* force_kernel_batched_symbol();
 // Resident blocks per SM of the two neighbour passes (single-scene or batched variant).
 void sph_occupancy(bool batched, int* density_blocks, int* force_blocks);
+
+// Internals of a wc_fluid, for the surrogate (wc_surrogate.cu), which works on a fluid's buffers.
+struct FluidInternals {
+    DevBuffers* d;
+    const SceneConsts* sc;
+    StepInputs* in;
+    const wc_params* params;
+    cudaStream_t stream;
+};
+FluidInternals fluid_internals(wc_fluid* f);
+void fluid_enqueue_sort(wc_fluid* f);
+wc_status fluid_graph_step(wc_fluid* f, float dt);  // one plain SPH step (graph replay)
+void fluid_count_step(wc_fluid* f);
 
 SceneConsts make_scene_consts(const wc_params& p);
 StepInputs make_step_inputs(const wc_params& p, float dt);

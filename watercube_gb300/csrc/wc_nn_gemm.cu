@@ -235,7 +235,9 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
         }
         if (g.c_f32) {
             float* out = g.c_f32 + (size_t)kz * g.split_stride + (size_t)row * g.ldc + col0;
-            if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
+            if (g.accumulate) {
+                for (uint32_t j = 0; j < ncols; ++j) out[j] += x[j];
+            } else if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
 #pragma unroll
                 for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(out + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
             } else {
@@ -285,7 +287,9 @@ wc_status check_gemm(const GemmArgs& g) {
     if (g.a_transposed && (g.lda % 8 || g.m % 8)) return fail(WC_ERR_INVALID_ARG, "gemm: transposed A needs m, lda %% 8 == 0");
     if (!g.b_rowmajor && g.ldb % 8) return fail(WC_ERR_INVALID_ARG, "gemm: B^T rows need ldb %% 8 == 0");
     if (g.b_rowmajor && (g.ldb % 8 || g.n % 8)) return fail(WC_ERR_INVALID_ARG, "gemm: row-major B needs n, ldb %% 8 == 0");
-    if (g.k % 8) return fail(WC_ERR_INVALID_ARG, "gemm: k must be a multiple of 8 (pad with zeros)");
+    // Both operands staged along k (transposed A, row-major B) read single k rows: any k works.
+    if (g.k % 8 && !(g.a_transposed && g.b_rowmajor))
+        return fail(WC_ERR_INVALID_ARG, "gemm: k must be a multiple of 8 (pad with zeros)");
     if ((g.add1 && !g.add1_idx) || (g.add2 && !g.add2_idx)) return fail(WC_ERR_INVALID_ARG, "gemm: gather without index");
     if (g.k_chunk == 0 || g.k_chunk % BK) return fail(WC_ERR_INVALID_ARG, "gemm: k_chunk must be a multiple of 64");
     return WC_OK;
@@ -335,6 +339,7 @@ extern "C" WC_API wc_status wc_nn_gemm(const wc_gemm_desc* d, uint32_t* d_err, v
     g.ld_add = d->ld_add;
     g.relu = d->relu;
     g.c_f32 = d->c_f32;
+    g.accumulate = d->accumulate;
     g.c_bf16 = static_cast<__nv_bfloat16*>(d->c_bf16);
     g.ldc = d->ldc;
     g.split_stride = d->split_stride;

@@ -444,7 +444,8 @@ __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t c
 __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const StepInputs& in, const float4& pi,
                                                 const float4& vi, const float f[6], uint32_t ti,
                                                 float4* __restrict__ pos_a, float4* __restrict__ vel_a,
-                                                const uint32_t* __restrict__ ids_b, uint32_t* __restrict__ ids_a) {
+                                                const uint32_t* __restrict__ ids_b, uint32_t* __restrict__ ids_a,
+                                               float4* __restrict__ accel) {
     const float fp_scale = -sc.m * sc.cs;         // -m * spiky const
     const float fv_scale = sc.m * sc.cv * sc.mu;  // m * visc const * mu
     const float rho = pi.w, pressure = vi.w;
@@ -459,11 +460,12 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     }
     const float inv = 1.f / (rho + 1e-16f);
     const float vin[3] = {vi.x, vi.y, vi.z};
-    float v[3], x[3];
+    float v[3], x[3], acc[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float force = fp_scale * f[a] + fv_scale * f[3 + a] + ext[a];
-        float va = vin[a] + (force * inv) * in.dt;
+        acc[a] = force * inv;
+        float va = vin[a] + acc[a] * in.dt;
         if (sc.flags & WC_FLAG_SPEED_CLAMP) va = fminf(fmaxf(va, -sc.max_speed), sc.max_speed);
         float xa = p3[a] + va * in.dt;
         if (xa < sc.border) {
@@ -479,6 +481,7 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     pos_a[ti] = make_float4(x[0], x[1], x[2], rho);
     vel_a[ti] = make_float4(v[0], v[1], v[2], pressure);
     if (ids_a) ids_a[ti] = ids_b[ti];
+    if (accel) accel[ti] = make_float4(acc[0], acc[1], acc[2], 0.f);
 }
 
 template <bool BATCHED>
@@ -493,7 +496,8 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts
                                                                const uint32_t* __restrict__ start,
                                                                const uint32_t* __restrict__ cell_list,
                                                                const uint32_t* __restrict__ num_nonempty,
-                                                               const uint32_t* __restrict__ hits) {
+                                                               const uint32_t* __restrict__ hits,
+                                                               float4* __restrict__ accel) {
     __shared__ uint32_t s_slot[WARPS][STAGE_CAP];             // candidate number -> sorted slot
     __shared__ uint32_t s_lists[WARPS][FORCE_LIST_CAP * 32];  // direct path: per-lane lists
     __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
@@ -578,7 +582,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts
             }
 #pragma unroll
             for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
-            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a);
+            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
             __syncwarp();  // the slot table is rewritten for the next cell
             continue;
         }
@@ -619,7 +623,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts
             accumulate_list(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
 #pragma unroll
             for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
-            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a);
+            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
         }
     }
 }
@@ -662,7 +666,7 @@ void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& 
                   cudaStream_t s) {
     force_kernel<false><<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, BatchTables{}, in, d.n, d.num_cells, d.pos_b,
                                                               d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
-                                                              d.cell_list, d.num_nonempty, d.hits);
+                                                              d.cell_list, d.num_nonempty, d.hits, d.accel);
 }
 
 void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
@@ -675,7 +679,7 @@ void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const Step
                           cudaStream_t s) {
     force_kernel<true><<<ld.grid_force, SPH_THREADS, 0, s>>>(SceneConsts{}, bt, in, d.n, d.num_cells, d.pos_b,
                                                              d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
-                                                             d.cell_list, d.num_nonempty, d.hits);
+                                                             d.cell_list, d.num_nonempty, d.hits, d.accel);
 }
 
 const void* force_kernel_symbol(uint32_t) { return reinterpret_cast<const void*>(&force_kernel<false>); }

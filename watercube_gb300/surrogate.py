@@ -1,0 +1,243 @@
+"""The learned message-passing surrogate over the C ABI (wc_surrogate_*), its training data from
+batched-solver trajectories, the training loop and the judged rollout. No counterpart in the
+reference, which only runs plain SPH.
+
+Network and kernels live in csrc/wc_surrogate.cu (driver), csrc/wc_nn_gemm.cu (tcgen05 GEMM) and
+csrc/wc_nn_ops.cu (graph, features, LayerNorm, reductions, Adam); this module only moves host
+arrays and drives the loop.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi as A
+from ._abi import RolloutStats, SurrogateConfig, check, lib
+from .batch import Batch, scene_params, scene_particles
+from .fluid import Fluid
+
+WC_ROLLOUT_SPH = 0
+WC_ROLLOUT_SURROGATE = 1
+WC_ROLLOUT_STALE = 2
+HISTORY = 5  # velocities per node feature (current + 4 previous)
+
+
+def default_config(**overrides) -> SurrogateConfig:
+    c = SurrogateConfig()
+    lib().wc_surrogate_config_default(C.byref(c))
+    for k, v in overrides.items():
+        setattr(c, k, v)
+    return c
+
+
+class Surrogate:
+    """One network with its FP32 master weights, Adam state and activation workspaces."""
+
+    def __init__(self, config: SurrogateConfig | None = None, **overrides):
+        cfg = config if config is not None else default_config(**overrides)
+        h = C.c_void_p()
+        check(lib().wc_surrogate_create(C.byref(cfg), C.byref(h)), "wc_surrogate_create")
+        self._h = h
+        self.config = cfg
+        self.num_params = int(lib().wc_surrogate_num_params(h))
+        self._n = 0
+
+    # ---- parameters --------------------------------------------------------------------------
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(lib().wc_surrogate_get_params(self._h, A._ptr(out), self.num_params), "get_params")
+        return out
+
+    def set_params(self, w: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        check(lib().wc_surrogate_set_params(self._h, A._ptr(w), w.size), "set_params")
+
+    def grads(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(lib().wc_surrogate_get_grads(self._h, A._ptr(out), self.num_params), "get_grads")
+        return out
+
+    def zero_grads(self) -> None:
+        check(lib().wc_surrogate_zero_grads(self._h), "zero_grads")
+
+    # ---- one sample ----------------------------------------------------------------------------
+    def sample(self, fluid: Fluid, hist: np.ndarray, target: np.ndarray | None = None) -> None:
+        """Load the fluid's current particles with their velocity history hist (5, n, 4) and
+        optional target accelerations (n, 4), both in the fluid's state order."""
+        n = fluid.numParticles()
+        hist = np.ascontiguousarray(hist, dtype=np.float32)
+        if hist.shape != (HISTORY, n, 4):
+            raise A.WatercubeError(A.WC_ERR_INVALID_ARG, f"history has shape {hist.shape}, want (5, {n}, 4)")
+        tp = None
+        if target is not None:
+            target = np.ascontiguousarray(target, dtype=np.float32)
+            if target.shape != (n, 4):
+                raise A.WatercubeError(A.WC_ERR_INVALID_ARG, f"target has shape {target.shape}")
+            tp = A._ptr(target)
+        check(lib().wc_surrogate_sample(self._h, fluid._require(), A._ptr(hist), tp), "wc_surrogate_sample")
+        self._n = n
+
+    def forward_backward(self, backward: bool = True) -> float:
+        loss = C.c_double(0.0)
+        check(lib().wc_surrogate_forward_backward(self._h, int(backward), C.byref(loss)), "forward_backward")
+        return loss.value
+
+    def predictions(self) -> np.ndarray:
+        out = np.zeros((self._n, 4), np.float32)
+        check(lib().wc_surrogate_predictions(self._h, A._ptr(out), self._n), "predictions")
+        return out
+
+    def adam(self, lr: float, grad_scale: float = 1.0) -> None:
+        check(lib().wc_surrogate_adam(self._h, float(lr), float(grad_scale)), "adam")
+
+    # ---- rollout -------------------------------------------------------------------------------
+    def rollout(self, fluid: Fluid, dt: float, nsteps: int, K: int = 4, tolerance: float = 0.01,
+                mode: int = WC_ROLLOUT_SURROGATE) -> dict:
+        return rollout(fluid, dt, nsteps, K, tolerance, mode, self)
+
+    def close(self) -> None:
+        if self._h is not None:
+            lib().wc_surrogate_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def rollout(fluid: Fluid, dt: float, nsteps: int, K: int = 4, tolerance: float = 0.01,
+            mode: int = WC_ROLLOUT_SPH, surrogate: Surrogate | None = None) -> dict:
+    """Advance `fluid` nsteps in `mode` (WC_ROLLOUT_*) and return the rollout statistics."""
+    st = RolloutStats()
+    h = surrogate._h if surrogate is not None else None
+    check(lib().wc_surrogate_rollout(h, fluid._require(), float(dt), int(nsteps), int(K), float(tolerance),
+                                     int(mode), C.byref(st)), "wc_surrogate_rollout")
+    return st.as_dict()
+
+
+# ---- training data ---------------------------------------------------------------------------
+
+@dataclass
+class Sample:
+    """One scene at one time step, arrays in particle-id order."""
+
+    scene: int
+    step: int
+    state: np.ndarray   # (n,) PARTICLE_DTYPE: positions and velocities before the step
+    hist: np.ndarray    # (5, n, 4) velocities, hist[0] = state velocity
+    target: np.ndarray  # (n, 4) SPH acceleration of the state (w = 0)
+
+
+def record_samples(specs, steps: int, dt: float, every: int = 1, start: int = 0) -> tuple[list, list[Sample]]:
+    """Run the batched solver on `specs` for `steps` steps with acceleration recording on and
+    collect one Sample per scene every `every` steps from step `start`. Returns (params per
+    scene, samples)."""
+    params = [scene_params(s) for s in specs]
+    initial = [scene_particles(s, p) for s, p in zip(specs, params)]
+    samples: list[Sample] = []
+    with Batch(params, initial) as b:
+        total = b.num_particles
+        off = b.offsets().astype(np.int64)
+        check(lib().wc_batch_set_recording(b._h, 1), "wc_batch_set_recording")
+        ids = np.zeros(total, np.uint32)
+        acc = np.zeros((total, 4), np.float32)
+        vel_by_id = np.zeros((total, 4), np.float32)
+        state = b.particles()
+        check(lib().wc_batch_get_ids(b._h, A._ptr(ids), total), "wc_batch_get_ids")
+        vel_by_id[ids, :3] = state["velocity"]
+        hist = np.repeat(vel_by_id[None], HISTORY, axis=0)
+        for t in range(steps):
+            state_by_id = np.empty(total, A.PARTICLE_DTYPE)
+            state_by_id[ids] = state
+            b.step(dt, 1)
+            check(lib().wc_batch_get_accelerations(b._h, A._ptr(acc), total), "wc_batch_get_accelerations")
+            check(lib().wc_batch_get_ids(b._h, A._ptr(ids), total), "wc_batch_get_ids")
+            acc_by_id = np.zeros((total, 4), np.float32)
+            acc_by_id[ids, :3] = acc[:, :3]
+            if t >= start and (t - start) % every == 0:
+                for s in range(len(specs)):
+                    lo, hi = int(off[s]), int(off[s + 1])
+                    samples.append(Sample(s, t, state_by_id[lo:hi].copy(), hist[:, lo:hi].copy(),
+                                          acc_by_id[lo:hi].copy()))
+            state = b.particles()
+            vel_by_id = np.zeros((total, 4), np.float32)
+            vel_by_id[ids, :3] = state["velocity"]
+            hist = np.concatenate([vel_by_id[None], hist[:-1]], axis=0)
+    return params, samples
+
+
+class Trainer:
+    """Adam on batches of samples (gradients accumulated over the batch, averaged), one
+    wc_fluid per scene holding the sample's particles for the graph build."""
+
+    def __init__(self, surrogate: Surrogate, params: list, position_noise: float = 3e-4, seed: int = 0):
+        self.s = surrogate
+        self.params = params
+        self.noise = position_noise
+        self.rng = np.random.default_rng(seed)
+        self._fluids: dict[int, Fluid] = {}
+
+    def fluid(self, scene: int, state: np.ndarray) -> Fluid:
+        f = self._fluids.get(scene)
+        if f is None:
+            f = Fluid(f"scene{scene}", self.params[scene])
+            f.setup(state)
+            self._fluids[scene] = f
+        else:
+            f.set_particles(state)
+        return f
+
+    def load(self, smp: Sample, noise: bool) -> None:
+        state = smp.state
+        if noise and self.noise > 0:
+            state = state.copy()
+            state["position"] += self.rng.normal(0.0, self.noise, state["position"].shape).astype(np.float32)
+            size = self.params[smp.scene].size
+            border = self.params[smp.scene].wall_border
+            np.clip(state["position"], border, size - border, out=state["position"])
+        f = self.fluid(smp.scene, state)
+        self.s.sample(f, smp.hist, smp.target)
+
+    def step(self, batch: list[Sample], lr: float) -> float:
+        """One Adam step over `batch`; returns the mean loss."""
+        losses = []
+        for smp in batch:
+            self.load(smp, noise=True)
+            losses.append(self.s.forward_backward(True))
+        self.s.adam(lr, 1.0 / len(batch))
+        return float(np.mean(losses))
+
+    def evaluate(self, samples: list[Sample]) -> float:
+        """Mean loss over samples (no noise, no gradient)."""
+        out = []
+        for smp in samples:
+            self.load(smp, noise=False)
+            out.append(self.s.forward_backward(False))
+        return float(np.mean(out))
+
+    def predict(self, smp: Sample) -> np.ndarray:
+        self.load(smp, noise=False)
+        self.s.forward_backward(False)
+        return self.s.predictions()
+
+    def train(self, samples: list[Sample], steps: int, lr: float = 1e-4, batch: int = 8) -> list[float]:
+        hist = []
+        for _ in range(steps):
+            idx = self.rng.choice(len(samples), size=min(batch, len(samples)), replace=False)
+            hist.append(self.step([samples[i] for i in idx], lr))
+        return hist
+
+    def close(self) -> None:
+        for f in self._fluids.values():
+            f.close()
+        self._fluids.clear()
