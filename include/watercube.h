@@ -209,7 +209,8 @@ WC_API wc_status wc_fluid_set_gravity(wc_fluid* f, const float gravity[3]);
 
 /* util::getParticles (util.cpp:42-60): synchronise and copy n particles of a buffer to host. */
 WC_API wc_status wc_fluid_get_particles(wc_fluid* f, int buffer, wc_particle* out, uint32_t n);
-/* util::setParticles (util.cpp:74-78): overwrite a buffer from host. */
+/* util::setParticles (util.cpp:74-78): overwrite a buffer from host. With WC_FLAG_TRACK_IDS,
+   writing the state buffer restarts the particle ids at the uploaded order (id = index). */
 WC_API wc_status wc_fluid_set_particles(wc_fluid* f, int buffer, const wc_particle* in, uint32_t n);
 /* util::getUints (util.cpp:62-72): synchronise and copy an integer buffer (WC_UINTS_*). n must
    equal its length: num_particles, or num_cells for the two cell tables. */
@@ -359,7 +360,8 @@ WC_API wc_status wc_nn_gemm(const wc_gemm_desc* g, uint32_t* d_err, void* stream
 /*
  * No counterpart in the reference. A message-passing network over the radius-h graph of a
  * fluid (latent width 128, `layers` message-passing steps) predicts each particle's SPH
- * acceleration from its last five velocities, its wall distances and the scene's stiffness.
+ * acceleration from its last five velocities (the current one and four differences / dt),
+ * its wall distances and the scene's stiffness.
  * Inputs and outputs are in the fluid's state-buffer order; the network works in the sorted
  * order internally.
  */
@@ -384,9 +386,9 @@ WC_API wc_status wc_surrogate_get_grads(wc_surrogate* s, float* host, uint64_t n
 WC_API wc_status wc_surrogate_zero_grads(wc_surrogate* s);
 /* Load one training sample: the fluid's current particles (positions and velocities, set
    with wc_fluid_set_particles), the velocity history hist[5][n][4] (hist[0] = current
-   velocity, hist[k] = k steps ago) and, optionally, the target accelerations target[n][4].
-   Sorts the fluid and builds the graph and features. */
-WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, const float* hist, const float* target);
+   velocity, hist[k] = k steps ago, dt apart) and, optionally, the target accelerations
+   target[n][4]. Sorts the fluid and builds the graph and features. */
+WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, const float* hist, const float* target);
 /* Forward pass on the loaded sample; with do_backward, the gradients of the mean squared error
    (per component, outputs scaled by 1 / accel_scale) are added to the accumulated ones. *loss
    (may be NULL) receives that error. */
@@ -419,9 +421,11 @@ typedef struct wc_rollout_stats {
 /* Advance the fluid nsteps in `mode`. In the SURROGATE and STALE modes every K-th step is
    judged: SPH and the candidate both advance the same state, the SPH densities of the two next
    states are compared particle by particle, and the SPH state is kept (the step is reverted)
-   when the mean |rho_candidate / rho_SPH - 1| exceeds `tolerance`. s may be NULL for SPH. */
+   when the mean |rho_candidate / rho_SPH - 1| exceeds `tolerance`. s may be NULL for SPH.
+   hist (host, [5][n][4] in state order, as for wc_surrogate_sample) seeds the surrogate's
+   velocity history; NULL starts it as five copies of the current velocity. */
 WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t K,
-                                      float tolerance, int mode, wc_rollout_stats* stats);
+                                      float tolerance, int mode, const float* hist, wc_rollout_stats* stats);
 
 /* ---- cell sort without allocation ------------------------------------------------------ */
 

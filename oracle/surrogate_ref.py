@@ -17,8 +17,9 @@ this order (each block's weight is [in x out] row-major, then its bias):
     a  = accel_scale * d2 relu(d1 h)   (first 3 outputs)
 Graph: ordered pairs (i, j), i != j, with d2 <= cull, d2 = fma(dz, dz, fma(dy, dy, dx * dx)) in
 FP32 (cull = largest float whose square root is below h), edge features from receiver i to
-sender j. Features: node = 5 velocities / velocity_scale, 6 wall distances / h clipped to
-[0, 1], stiffness / rest density * 200, zeros to 32; edge = (x_i - x_j) / h, |x_i - x_j| / h,
+sender j. Features: node = current velocity / velocity_scale, the four successive velocity
+differences / (dt accel_scale) (FP32), 6 wall distances / h clipped to [0, 1], stiffness /
+rest density * 200, zeros to 32; edge = (x_i - x_j) / h, |x_i - x_j| / h,
 zeros to 16.
 
 Emulated BF16 rounding: the CUDA path keeps features, weights and the stored activations in
@@ -108,13 +109,16 @@ def radius_graph(pos: np.ndarray, cull: float) -> tuple[np.ndarray, np.ndarray]:
     return recv.astype(np.int64), send.astype(np.int64)
 
 
-def node_features(pos, hist, size, h, k_feature, velocity_scale) -> np.ndarray:
+def node_features(pos, hist, size, h, k_feature, velocity_scale, dt, accel_scale) -> np.ndarray:
     pos = np.asarray(pos, np.float32)
     n = pos.shape[0]
     f = np.zeros((n, NODE_IN), np.float32)
     inv_v = np.float32(1.0) / np.float32(velocity_scale)
-    for s in range(5):
-        f[:, 3 * s:3 * s + 3] = np.asarray(hist[s][:, :3], np.float32) * inv_v
+    inv_dv = np.float32(1.0) / (np.float32(dt) * np.float32(accel_scale))
+    v = [np.asarray(hist[s][:, :3], np.float32) for s in range(5)]
+    f[:, 0:3] = v[0] * inv_v
+    for s in range(1, 5):
+        f[:, 3 * s:3 * s + 3] = (v[s - 1] - v[s]) * inv_dv
     inv_h = np.float32(1.0) / np.float32(h)
     walls = [pos[:, 0], np.float32(size) - pos[:, 0], pos[:, 1], np.float32(size) - pos[:, 1], pos[:, 2],
              np.float32(size) - pos[:, 2]]
@@ -214,13 +218,13 @@ def cull_threshold(h: float) -> np.float32:
     return x
 
 
-def sample_inputs(state: np.ndarray, hist: np.ndarray, params, velocity_scale: float):
+def sample_inputs(state: np.ndarray, hist: np.ndarray, params, velocity_scale: float, dt: float, accel_scale: float):
     """Graph and features of one sample (state: PARTICLE_DTYPE, hist: (5, n, 4)), as the CUDA path
     builds them from the same particles."""
     pos = np.asarray(state["position"], np.float32)
     cull = cull_threshold(params.kernel_radius)
     recv, send = radius_graph(pos, cull)
     k_feature = np.float32(params.stiffness) / np.float32(params.rest_density) * np.float32(200.0)
-    xn = node_features(pos, hist, params.size, params.kernel_radius, k_feature, velocity_scale)
+    xn = node_features(pos, hist, params.size, params.kernel_radius, k_feature, velocity_scale, dt, accel_scale)
     xe = edge_features(pos, recv, send, params.kernel_radius)
     return xn, xe, recv, send

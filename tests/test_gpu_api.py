@@ -55,6 +55,22 @@ def test_host_copies_round_trip(gpu):
         assert f.particles(_abi.WC_BUFFER_SORTED).tobytes() == st2.tobytes()
 
 
+def test_set_particles_restarts_tracked_ids(gpu):
+    p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
+    with fluid(p, st) as f:
+        f.step(1e-3, 2)
+        ids = f.particle_ids()
+        assert not np.array_equal(ids, np.arange(len(ids)))  # the sort moved the particles
+        state = f.particles()
+        f.set_particles(state)
+        assert np.array_equal(f.particle_ids(), np.arange(len(ids)))
+        f.step(1e-3, 1)
+        out, ids2 = f.particles(), f.particle_ids()
+        assert np.array_equal(np.sort(ids2), np.arange(len(ids)))
+        moved = np.linalg.norm(out["position"] - state["position"][ids2], axis=1)
+        assert moved.max() < 0.01 * p.kernel_radius  # each id follows its own particle (spacing 0.5 h)
+
+
 def test_device_buffers(gpu):
     p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS | _abi.WC_FLAG_NEIGHBOR_COUNTS)
     with fluid(p, st) as f:

@@ -40,7 +40,8 @@ def scene(n: int, seed: int = 1):
     state["velocity"] = rng.normal(0.0, 0.3, (n, 3)).astype(np.float32)
     hist = np.zeros((5, n, 4), np.float32)
     hist[0, :, :3] = state["velocity"]
-    hist[1:, :, :3] = rng.normal(0.0, 0.3, (4, n, 3))
+    for k in range(1, 5):  # earlier velocities differ by accelerations of about 5 m/s^2 x dt
+        hist[k, :, :3] = hist[k - 1, :, :3] - rng.normal(0.0, 5.0, (n, 3)) * 1e-3
     target = np.zeros((n, 4), np.float32)
     target[:, :3] = rng.normal(0.0, 5.0, (n, 3))
     target[:, 1] -= 9.81
@@ -86,12 +87,12 @@ def test_gradients_match_fp64_oracle(gpu, layers, n):
         w = perturbed_params(s, seed=11)
         s.set_params(w)
         f.setup(state)
-        s.sample(f, hist, target)
+        s.sample(f, 1e-3, hist, target)
         s.zero_grads()
         loss = s.forward_backward(True)
         g = s.grads().astype(np.float64)
         pred = s.predictions()
-        xn, xe, recv, send = R.sample_inputs(state, hist, p, s.config.velocity_scale)
+        xn, xe, recv, send = R.sample_inputs(state, hist, p, s.config.velocity_scale, 1e-3, s.config.accel_scale)
         ref_loss, ref_g, ref_pred = R.Net(w, layers).loss_and_grads(xn, xe, recv, send, target, s.config.accel_scale)
     assert abs(loss - ref_loss) <= 1e-2 * ref_loss
     perr = np.linalg.norm(pred[:, :3] - ref_pred) / np.linalg.norm(ref_pred)
@@ -119,7 +120,7 @@ def test_gradients_accumulate_and_adam_moves_weights(gpu):
     p, state, hist, target = scene(1200, seed=5)
     with Surrogate(layers=2, seed=3) as s, Fluid("acc", p) as f:
         f.setup(state)
-        s.sample(f, hist, target)
+        s.sample(f, 1e-3, hist, target)
         s.zero_grads()
         s.forward_backward(True)
         g1 = s.grads()
@@ -143,7 +144,7 @@ def test_sample_rejects_bad_shapes(gpu):
     with Surrogate(layers=1) as s, Fluid("bad", p) as f:
         f.setup(state)
         with pytest.raises(_abi.WatercubeError):
-            s.sample(f, hist[:4], target)
+            s.sample(f, 1e-3, hist[:4], target)
         with pytest.raises(_abi.WatercubeError):
             s.forward_backward(True)  # nothing loaded yet
 
@@ -159,6 +160,77 @@ def test_rollout_sph_mode_matches_plain_steps(gpu):
         assert st["steps"] == 12 and st["sph_steps"] == 12 and st["judged"] == 0
         assert np.array_equal(a.particles(), b.particles())
         assert st["diag_start"][0] == st["diag_end"][0]
+
+
+def integrate_host(p, state, accel, dt):
+    """The surrogate step's integrator on the host (FP32): v += a dt, x += v dt, wall clamp."""
+    x = state["position"].astype(np.float32).copy()
+    v = state["velocity"].astype(np.float32).copy()
+    dt = np.float32(dt)
+    v = v + accel[:, :3].astype(np.float32) * dt
+    if p.flags & _abi.WC_FLAG_SPEED_CLAMP:
+        v = np.clip(v, -p.max_speed, p.max_speed)
+    x = x + v * dt
+    lo, hi = np.float32(p.wall_border), np.float32(p.size) - np.float32(p.wall_border)
+    for cond, wall in ((x < lo, lo), (x > hi, hi)):
+        v[cond] *= -np.float32(p.wall_damping)
+        x[cond] = wall
+    return x, v
+
+
+def test_rollout_surrogate_steps_follow_network_predictions(gpu):
+    """Two accepted surrogate steps of the rollout equal two steps made by hand from the
+    network's predictions (sample -> predictions -> host integrator), the second one with the
+    velocity history shifted by the first: the rollout's inference path, history and
+    integrator agree with the training path."""
+    dt = 1e-3
+    p, state, hist, _ = scene(3000, seed=8)
+    p.flags |= _abi.WC_FLAG_TRACK_IDS
+    with Surrogate(layers=2, seed=5) as s, Fluid("hand", p) as a, Fluid("roll", p) as b:
+        s.set_params(perturbed_params(s, seed=2))
+        a.setup(state)
+        b.setup(state)
+        cur, h = state.copy(), hist.copy()
+        for _ in range(2):
+            a.set_particles(cur)
+            s.sample(a, dt, h)
+            s.forward_backward(False)
+            pred = s.predictions()
+            x, v = integrate_host(p, cur, pred, dt)
+            cur = cur.copy()
+            cur["position"], cur["velocity"] = x, v
+            h = np.concatenate([np.pad(v, ((0, 0), (0, 1)))[None], h[:-1]], axis=0)
+        st = s.rollout(b, dt, 2, K=1, tolerance=1e9, mode=WC_ROLLOUT_SURROGATE, hist=hist)
+        assert st["reverted"] == 0 and st["judged"] == 2
+        out, ids = b.particles(), b.particle_ids()
+    got_x = np.empty_like(cur["position"])
+    got_v = np.empty_like(cur["velocity"])
+    got_x[ids] = out["position"]
+    got_v[ids] = out["velocity"]
+    # the kernel may contract v + a dt into one fma (a few ulps), and a last-bit difference in the
+    # second step's features may flip a BF16 rounding: far below a wrong step (~1e-2 m/s)
+    np.testing.assert_allclose(got_v, cur["velocity"], rtol=0, atol=3e-5)
+    np.testing.assert_allclose(got_x, cur["position"], rtol=0, atol=2e-7)
+
+
+@pytest.mark.parametrize("mode", [WC_ROLLOUT_SURROGATE, WC_ROLLOUT_STALE])
+@pytest.mark.parametrize("track_ids", [False, True])
+def test_rollout_reverting_every_step_is_plain_sph(gpu, mode, track_ids):
+    """K = 1 and tolerance 0 judge and revert every step: the state (and the particle ids) must
+    be bit-identical to plain SPH steps, whatever the candidate computed beside it."""
+    p = finalize(dam_break_params(4096))
+    if track_ids:
+        p.flags |= _abi.WC_FLAG_TRACK_IDS
+    state = generate_dam_break(p, 2)
+    with Surrogate(layers=2, seed=1) as s, Fluid("a", p) as a, Fluid("b", p) as b:
+        a.setup(state)
+        b.setup(state)
+        a.step(1e-3, 9)
+        st = s.rollout(b, 1e-3, 9, K=1, tolerance=0.0, mode=mode)
+        assert st["reverted"] == st["judged"] == (9 if mode == WC_ROLLOUT_SURROGATE else 8)
+        assert np.array_equal(a.particles(), b.particles())
+        if track_ids:
+            assert np.array_equal(a.particle_ids(), b.particle_ids())
 
 
 @pytest.mark.parametrize("mode", [WC_ROLLOUT_SURROGATE, WC_ROLLOUT_STALE])

@@ -50,9 +50,14 @@ def test_features():
     pos = np.array([[0.0, 0.5, 0.02], [0.99, 0.01, 0.5]], np.float32)
     hist = np.zeros((5, 2, 4), np.float32)
     hist[0, :, :3] = [[1.0, -2.0, 0.5], [0.0, 0.0, 3.0]]
-    xn = R.node_features(pos, hist, 1.0, p.kernel_radius, 7.0, 2.0)
+    hist[1, :, :3] = [[0.99, -2.0, 0.5], [0.0, 0.01, 3.0]]
+    xn = R.node_features(pos, hist, 1.0, p.kernel_radius, 7.0, 2.0, 1e-3, 10.0)
     assert xn.shape == (2, 32)
     assert np.allclose(xn[0, :3], [0.5, -1.0, 0.25])
+    assert np.allclose(xn[0, 3:6], [1.0, 0.0, 0.0], atol=1e-4)  # (v0 - v1) / (dt a_scale)
+    assert np.allclose(xn[1, 3:6], [0.0, -1.0, 0.0], atol=1e-4)
+    assert np.allclose(xn[:, 6:9], hist[1, :, :3] * 100.0, rtol=1e-5)  # v1 - v2 with v2 = 0
+    assert np.all(xn[:, 9:15] == 0.0)  # v2 - v3 = v3 - v4 = 0
     assert xn[0, 15] == 0.0 and xn[0, 16] == 1.0  # at the x = 0 wall; far from x = size
     assert xn[1, 16] == pytest.approx(0.01 / p.kernel_radius, rel=1e-5) or xn[1, 16] == 1.0
     assert np.all(xn[:, 21] == 7.0) and np.all(xn[:, 22:] == 0.0)
@@ -67,7 +72,7 @@ def small_case(layers, n=300, seed=0):
     hist = rng.normal(0.0, 0.3, (5, n, 4)).astype(np.float32)
     h = 0.05
     recv, send = R.radius_graph(pos, R.cull_threshold(h))
-    xn = R.node_features(pos, hist, 1.0, h, 0.6, 1.0)
+    xn = R.node_features(pos, hist, 1.0, h, 0.6, 1.0, 1e-3, 10.0)
     xe = R.edge_features(pos, recv, send, h)
     target = rng.normal(0.0, 5.0, (n, 4)).astype(np.float32)
     w = rng.normal(0.0, 0.08, R.num_params(layers))

@@ -298,16 +298,7 @@ WC_API wc_status wc_fluid_setup(wc_fluid* f, const wc_particle* initial, uint32_
     WC_TRY(require(f, false));
     if (n != f->d.n) return fail(WC_ERR_INVALID_ARG, "setup with %u particles, handle holds %u", n, f->d.n);
     if (n && !initial) return fail(WC_ERR_INVALID_ARG, "null initial particles");
-    if (n) {
-        WC_TRY(wc_fluid_set_particles(f, WC_BUFFER_STATE, initial, n));
-        if (f->d.ids_a) {
-            std::vector<uint32_t> iota(n);
-            for (uint32_t i = 0; i < n; ++i) iota[i] = i;
-            WC_CUDA_TRY(cudaMemcpyAsync(f->d.ids_a, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice,
-                                        f->stream));
-            WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
-        }
-    }
+    if (n) WC_TRY(wc_fluid_set_particles(f, WC_BUFFER_STATE, initial, n));
     f->setup_done = true;
     f->steps = 0;
     return WC_OK;
@@ -402,6 +393,12 @@ WC_API wc_status wc_fluid_set_particles(wc_fluid* f, int buffer, const wc_partic
     const bool st = buffer == WC_BUFFER_STATE;
     launch_aos_to_soa(f->staging, st ? f->d.pos_a : f->d.pos_b, st ? f->d.vel_a : f->d.vel_b, n, f->stream);
     WC_TRY(check_launch());
+    if (st && f->d.ids_a) {
+        // tracked ids restart at the uploaded order
+        std::vector<uint32_t> iota(n);
+        for (uint32_t i = 0; i < n; ++i) iota[i] = i;
+        WC_CUDA_TRY(cudaMemcpyAsync(f->d.ids_a, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, f->stream));
+    }
     // The host buffer may be reused as soon as this returns.
     WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
     return WC_OK;

@@ -54,8 +54,8 @@ void graph_count(const float4* pos, uint32_t n, const uint32_t* start, float bin
 void graph_fill(const float4* pos, uint32_t n, const uint32_t* start, float bin, int32_t R, float cull,
                 const uint32_t* rowptr, uint32_t* col, cudaStream_t s);
 void graph_rev(uint32_t n, const uint32_t* rowptr, const uint32_t* col, uint32_t* recv, uint32_t* rev, cudaStream_t s);
-void node_features(uint32_t n, const float4* pos, const float4* hist, float inv_v, float inv_h, float size,
-                   float k_feature, __nv_bfloat16* out, cudaStream_t s);
+void node_features(uint32_t n, const float4* pos, const float4* hist, float inv_v, float inv_dv, float inv_h,
+                   float size, float k_feature, __nv_bfloat16* out, cudaStream_t s);
 void edge_features(uint32_t e, const float4* pos, const uint32_t* recv, const uint32_t* col, float inv_h,
                    __nv_bfloat16* out, cudaStream_t s);
 void layernorm(uint32_t rows, const float* y, const float* gamma, const float* beta, const __nv_bfloat16* resid,

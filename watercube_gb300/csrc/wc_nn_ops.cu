@@ -91,20 +91,28 @@ __global__ void graph_rev_kernel(uint32_t n, const uint32_t* __restrict__ rowptr
 
 // ---- features ---------------------------------------------------------------------------------
 
-// Node features (32, bf16): 5 velocities / v_scale (15), wall distances / h clipped to 1 (6),
-// stiffness / rest density * 200 (1), zeros (10). hist[s * n + i] is the velocity s steps ago.
+// Node features (32, bf16): the last 5 velocities as the current velocity / v_scale (3) and the
+// four successive differences (v[s-1] - v[s]) * inv_dv (12; inv_dv = 1 / (dt a_scale), so each is
+// a past acceleration on the output scale), wall distances / h clipped to 1 (6), stiffness /
+// rest density * 200 (1), zeros (10). hist[s * n + i] is the velocity s steps ago. The
+// differences are taken in FP32 before the BF16 cast, which would otherwise lose them.
 __global__ void node_features_kernel(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ hist,
-                                     float inv_v, float inv_h, float size, float k_feature,
+                                     float inv_v, float inv_dv, float inv_h, float size, float k_feature,
                                      __nv_bfloat16* __restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float f[32];
+    float4 prev = hist[i];
+    f[0] = prev.x * inv_v;
+    f[1] = prev.y * inv_v;
+    f[2] = prev.z * inv_v;
 #pragma unroll
-    for (int s = 0; s < 5; ++s) {
+    for (int s = 1; s < 5; ++s) {
         const float4 v = hist[(size_t)s * n + i];
-        f[3 * s] = v.x * inv_v;
-        f[3 * s + 1] = v.y * inv_v;
-        f[3 * s + 2] = v.z * inv_v;
+        f[3 * s] = (prev.x - v.x) * inv_dv;
+        f[3 * s + 1] = (prev.y - v.y) * inv_dv;
+        f[3 * s + 2] = (prev.z - v.z) * inv_dv;
+        prev = v;
     }
     const float4 p = pos[i];
     const float w[6] = {p.x, size - p.x, p.y, size - p.y, p.z, size - p.z};
@@ -421,9 +429,11 @@ void graph_fill(const float4* pos, uint32_t n, const uint32_t* start, float bin,
 void graph_rev(uint32_t n, const uint32_t* rowptr, const uint32_t* col, uint32_t* recv, uint32_t* rev, cudaStream_t s) {
     if (n) graph_rev_kernel<<<blocks_for(n, 128), 128, 0, s>>>(n, rowptr, col, recv, rev);
 }
-void node_features(uint32_t n, const float4* pos, const float4* hist, float inv_v, float inv_h, float size,
-                   float k_feature, __nv_bfloat16* out, cudaStream_t s) {
-    if (n) node_features_kernel<<<blocks_for(n, 128), 128, 0, s>>>(n, pos, hist, inv_v, inv_h, size, k_feature, out);
+void node_features(uint32_t n, const float4* pos, const float4* hist, float inv_v, float inv_dv, float inv_h,
+                   float size, float k_feature, __nv_bfloat16* out, cudaStream_t s) {
+    if (n)
+        node_features_kernel<<<blocks_for(n, 128), 128, 0, s>>>(n, pos, hist, inv_v, inv_dv, inv_h, size, k_feature,
+                                                                out);
 }
 void edge_features(uint32_t e, const float4* pos, const uint32_t* recv, const uint32_t* col, float inv_h,
                    __nv_bfloat16* out, cudaStream_t s) {

@@ -139,6 +139,7 @@ struct wc_surrogate {
     wc_fluid* fluid = nullptr;
     uint32_t n = 0, e = 0;
     bool has_target = false;
+    float dt = 1e-3f;  // time step of the loaded sample (velocity differences / dt are features)
     float4* hist_in = nullptr;  // [5 n] in state order (sample / rollout history)
     float4* target_in = nullptr;
     uint32_t cap_in = 0;
@@ -446,8 +447,9 @@ wc_status prepare_sample(wc_surrogate* s, wc_fluid* f, bool saved) {
     for (int k = 0; k < 5; ++k) gather4(n, d.perm, s->hist_in + (size_t)k * n, w.hist_s + (size_t)k * n, s->stream);
     if (s->has_target) gather4(n, d.perm, s->target_in, w.target_s, s->stream);
     const float k_feature = fi.params->stiffness / fi.params->rest_density * 200.0f;
-    node_features(n, d.pos_b, w.hist_s, 1.0f / s->cfg.velocity_scale, 1.0f / fi.sc->h, fi.sc->size, k_feature, w.xn,
-                  s->stream);
+    const float inv_dv = 1.0f / (s->dt * s->cfg.accel_scale);
+    node_features(n, d.pos_b, w.hist_s, 1.0f / s->cfg.velocity_scale, inv_dv, 1.0f / fi.sc->h, fi.sc->size, k_feature,
+                  w.xn, s->stream);
     edge_features(e, d.pos_b, w.recv, w.col, 1.0f / fi.sc->h, w.xe, s->stream);
     s->n = n;
     s->e = e;
@@ -648,6 +650,7 @@ struct RolloutRun {
     float tolerance;
     int mode;
     wc_rollout_stats* out;
+    const float* host_hist;  // initial velocity history, or null
     LaunchDims dims{};
     double err_sum = 0.0, err_max = 0.0;
 
@@ -679,6 +682,9 @@ struct RolloutRun {
         DevBuffers tgt = D;
         tgt.pos_a = dst_pos;
         tgt.vel_a = dst_vel;
+        // A candidate written beside the state buffer leaves its ids alone: they must keep
+        // matching the state's particles, which the judge's SPH step sorts next.
+        if (dst_pos != D.pos_a) tgt.ids_a = nullptr;
         integrate(D.n, *fi.sc, dt, acc, ld, scale, tgt, fi.stream);
         return WC_OK;
     }
@@ -739,8 +745,13 @@ struct RolloutRun {
         int device = 0;
         WC_CUDA_TRY(cudaGetDevice(&device));
         dims = compute_launch_dims(device);
-        // history starts as five copies of the current velocity
-        for (int k = 0; k < 5; ++k) WC_TRY(copy(s->hist_in + (size_t)k * n, D.vel_a));
+        if (host_hist) {
+            WC_CUDA_TRY(cudaMemcpyAsync(s->hist_in, host_hist, sizeof(float4) * 5 * (size_t)n, cudaMemcpyHostToDevice,
+                                        fi.stream));
+        } else {
+            // history starts as five copies of the current velocity
+            for (int k = 0; k < 5; ++k) WC_TRY(copy(s->hist_in + (size_t)k * n, D.vel_a));
+        }
         s->has_target = false;
         cudaEvent_t e0, e1;
         WC_CUDA_TRY(cudaEventCreate(&e0));
@@ -905,9 +916,12 @@ WC_API wc_status wc_surrogate_zero_grads(wc_surrogate* s) {
     return WC_OK;
 }
 
-WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, const float* host_hist, const float* host_target) {
+WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, const float* host_hist,
+                                     const float* host_target) {
     clear_error();
     if (!s || !f || !host_hist) return fail(WC_ERR_INVALID_ARG, "null argument");
+    if (!(dt > 0.f)) return fail(WC_ERR_INVALID_ARG, "dt must be > 0");
+    s->dt = dt;
     FluidInternals fi = fluid_internals(f);
     const uint32_t n = fi.d->n;
     WC_TRY(ensure_inputs(s, n));
@@ -976,7 +990,7 @@ WC_API wc_status wc_surrogate_adam(wc_surrogate* s, float lr, float grad_scale) 
 }
 
 WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t K,
-                                      float tolerance, int mode, wc_rollout_stats* out) {
+                                      float tolerance, int mode, const float* hist, wc_rollout_stats* out) {
     clear_error();
     if (!out) return fail(WC_ERR_INVALID_ARG, "null argument");
     std::memset(out, 0, sizeof *out);
@@ -1041,7 +1055,8 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
     WC_TRY(fluid_diag(f, out->diag_start));
     cudaStream_t own = s->stream;
     s->stream = fi.stream;  // everything runs on the fluid's stream
-    RolloutRun run{s, f, fi, dt, K, tolerance, mode, out};
+    s->dt = dt;
+    RolloutRun run{s, f, fi, dt, K, tolerance, mode, out, hist};
     const wc_status rc = run.go(nsteps);
     s->stream = own;
     s->fluid = nullptr;  // the loaded sample was replaced by the rollout's graphs

@@ -63,9 +63,9 @@ class Surrogate:
         check(lib().wc_surrogate_zero_grads(self._h), "zero_grads")
 
     # ---- one sample ----------------------------------------------------------------------------
-    def sample(self, fluid: Fluid, hist: np.ndarray, target: np.ndarray | None = None) -> None:
-        """Load the fluid's current particles with their velocity history hist (5, n, 4) and
-        optional target accelerations (n, 4), both in the fluid's state order."""
+    def sample(self, fluid: Fluid, dt: float, hist: np.ndarray, target: np.ndarray | None = None) -> None:
+        """Load the fluid's current particles with their velocity history hist (5, n, 4), steps
+        dt apart, and optional target accelerations (n, 4), both in the fluid's state order."""
         n = fluid.numParticles()
         hist = np.ascontiguousarray(hist, dtype=np.float32)
         if hist.shape != (HISTORY, n, 4):
@@ -76,7 +76,7 @@ class Surrogate:
             if target.shape != (n, 4):
                 raise A.WatercubeError(A.WC_ERR_INVALID_ARG, f"target has shape {target.shape}")
             tp = A._ptr(target)
-        check(lib().wc_surrogate_sample(self._h, fluid._require(), A._ptr(hist), tp), "wc_surrogate_sample")
+        check(lib().wc_surrogate_sample(self._h, fluid._require(), float(dt), A._ptr(hist), tp), "wc_surrogate_sample")
         self._n = n
 
     def forward_backward(self, backward: bool = True) -> float:
@@ -94,8 +94,8 @@ class Surrogate:
 
     # ---- rollout -------------------------------------------------------------------------------
     def rollout(self, fluid: Fluid, dt: float, nsteps: int, K: int = 4, tolerance: float = 0.01,
-                mode: int = WC_ROLLOUT_SURROGATE) -> dict:
-        return rollout(fluid, dt, nsteps, K, tolerance, mode, self)
+                mode: int = WC_ROLLOUT_SURROGATE, hist: np.ndarray | None = None) -> dict:
+        return rollout(fluid, dt, nsteps, K, tolerance, mode, self, hist)
 
     def close(self) -> None:
         if self._h is not None:
@@ -116,12 +116,19 @@ class Surrogate:
 
 
 def rollout(fluid: Fluid, dt: float, nsteps: int, K: int = 4, tolerance: float = 0.01,
-            mode: int = WC_ROLLOUT_SPH, surrogate: Surrogate | None = None) -> dict:
-    """Advance `fluid` nsteps in `mode` (WC_ROLLOUT_*) and return the rollout statistics."""
+            mode: int = WC_ROLLOUT_SPH, surrogate: Surrogate | None = None, hist: np.ndarray | None = None) -> dict:
+    """Advance `fluid` nsteps in `mode` (WC_ROLLOUT_*) and return the rollout statistics. `hist`
+    (5, n, 4), in the fluid's state order, seeds the surrogate's velocity history."""
     st = RolloutStats()
     h = surrogate._h if surrogate is not None else None
+    hp = None
+    if hist is not None:
+        hist = np.ascontiguousarray(hist, dtype=np.float32)
+        if hist.shape != (HISTORY, fluid.numParticles(), 4):
+            raise A.WatercubeError(A.WC_ERR_INVALID_ARG, f"history has shape {hist.shape}")
+        hp = A._ptr(hist)
     check(lib().wc_surrogate_rollout(h, fluid._require(), float(dt), int(nsteps), int(K), float(tolerance),
-                                     int(mode), C.byref(st)), "wc_surrogate_rollout")
+                                     int(mode), hp, C.byref(st)), "wc_surrogate_rollout")
     return st.as_dict()
 
 
@@ -133,6 +140,7 @@ class Sample:
 
     scene: int
     step: int
+    dt: float
     state: np.ndarray   # (n,) PARTICLE_DTYPE: positions and velocities before the step
     hist: np.ndarray    # (5, n, 4) velocities, hist[0] = state velocity
     target: np.ndarray  # (n, 4) SPH acceleration of the state (w = 0)
@@ -167,7 +175,7 @@ def record_samples(specs, steps: int, dt: float, every: int = 1, start: int = 0)
             if t >= start and (t - start) % every == 0:
                 for s in range(len(specs)):
                     lo, hi = int(off[s]), int(off[s + 1])
-                    samples.append(Sample(s, t, state_by_id[lo:hi].copy(), hist[:, lo:hi].copy(),
+                    samples.append(Sample(s, t, dt, state_by_id[lo:hi].copy(), hist[:, lo:hi].copy(),
                                           acc_by_id[lo:hi].copy()))
             state = b.particles()
             vel_by_id = np.zeros((total, 4), np.float32)
@@ -180,10 +188,14 @@ class Trainer:
     """Adam on batches of samples (gradients accumulated over the batch, averaged), one
     wc_fluid per scene holding the sample's particles for the graph build."""
 
-    def __init__(self, surrogate: Surrogate, params: list, position_noise: float = 3e-4, seed: int = 0):
+    def __init__(self, surrogate: Surrogate, params: list, position_noise: float = 3e-4, seed: int = 0,
+                 velocity_noise: float = 0.0):
         self.s = surrogate
         self.params = params
         self.noise = position_noise
+        # independent Gaussian noise on each velocity of the history (the state's velocity is
+        # hist[0] and moves with it): robustness to the network's own past errors in a rollout
+        self.vnoise = velocity_noise
         self.rng = np.random.default_rng(seed)
         self._fluids: dict[int, Fluid] = {}
 
@@ -198,7 +210,12 @@ class Trainer:
         return f
 
     def load(self, smp: Sample, noise: bool) -> None:
-        state = smp.state
+        state, hist = smp.state, smp.hist
+        if noise and self.vnoise > 0:
+            hist = hist + np.pad(self.rng.normal(0.0, self.vnoise, hist[..., :3].shape),
+                                 ((0, 0), (0, 0), (0, 1))).astype(np.float32)
+            state = state.copy()
+            state["velocity"] = hist[0, :, :3]
         if noise and self.noise > 0:
             state = state.copy()
             state["position"] += self.rng.normal(0.0, self.noise, state["position"].shape).astype(np.float32)
@@ -206,7 +223,7 @@ class Trainer:
             border = self.params[smp.scene].wall_border
             np.clip(state["position"], border, size - border, out=state["position"])
         f = self.fluid(smp.scene, state)
-        self.s.sample(f, smp.hist, smp.target)
+        self.s.sample(f, smp.dt, hist, smp.target)
 
     def step(self, batch: list[Sample], lr: float) -> float:
         """One Adam step over `batch`; returns the mean loss."""
