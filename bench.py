@@ -15,6 +15,10 @@ cpu_baseline  the CPU transcription of the reference's stages (oracle, FP32) on 
            cores, on a bounded sample of the same workload.
 --impl reference  times the reference's own shader code compiled for the host CPU
            (oracle/_ref, when built) or else the oracle's transcription, all threads.
+rollout    the judged rollout at the same size from the same initial state (plain SPH, the
+           learned surrogate with an SPH judge every K = 4 steps, and the stale-acceleration
+           method without the network), a bounded number of steps each; `--workload rollout1m`
+           times it alone with --steps steps.
 Multi-GPU (torchrun): every rank runs an independent replica (the path has no exchange step);
 the slowest rank's time is reported.
 """
@@ -251,6 +255,74 @@ def run_reference(args):
     return 0
 
 
+def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01) -> dict:
+    """Plain SPH, surrogate and stale-acceleration rollouts of `steps` steps from `st`, each on a
+    fresh fluid; the surrogate uses the committed trained weights when present."""
+    from watercube_gb300.fluid import Fluid
+    from watercube_gb300.surrogate import WC_ROLLOUT_SPH, WC_ROLLOUT_STALE, WC_ROLLOUT_SURROGATE, Surrogate, rollout
+    from watercube_gb300.train_surrogate import DEFAULT_WEIGHTS, load_weights
+
+    trained = DEFAULT_WEIGHTS.is_file()
+    s = load_weights() if trained else Surrogate(layers=8, seed=1)
+    out = {"steps": steps, "K": K, "tolerance": tolerance,
+           "weights": DEFAULT_WEIGHTS.relative_to(REPO).as_posix() if trained else "untrained (seed 1)"}
+    keep = ("particle_steps_per_s", "ms_device", "sph_steps", "surrogate_steps", "judged", "reverted",
+            "mean_density_error", "max_density_error")
+    for mode, name in ((WC_ROLLOUT_SPH, "plain"), (WC_ROLLOUT_SURROGATE, "surrogate"), (WC_ROLLOUT_STALE, "stale")):
+        f = Fluid.create("rollout", p)
+        f.setup(st)
+        if mode == WC_ROLLOUT_SURROGATE:
+            rollout(f, dt, 1, K, tolerance, mode, s)  # workspace allocation outside the timed rollout
+            f.setup(st)
+        else:
+            rollout(f, dt, 2, K, tolerance, mode, s)  # graph capture
+            f.setup(st)
+        r = rollout(f, dt, steps, K, tolerance, mode, s)
+        d0, d1 = np.array(r["diag_start"]), np.array(r["diag_end"])
+        e = {k: r[k] for k in keep}
+        e["momentum_change"] = float(np.linalg.norm(d1[1:4] - d0[1:4]))  # gravity and walls act on it
+        e["energy_change_rel"] = float(abs((d1[4] + d1[5]) - (d0[4] + d0[5])) / max(abs(d0[4] + d0[5]), 1e-30))
+        out[name] = e
+        f.close()
+    s.close()
+    out["surrogate_vs_plain"] = out["surrogate"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
+    out["stale_vs_plain"] = out["stale"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
+    return out
+
+
+def run_rollout_workload(args):
+    """--workload rollout1m: the judged rollouts at 1,048,576 particles from the dam break's initial
+    state, --steps steps each (dt = 2.5e-4, K = 4, 1% density tolerance)."""
+    from watercube_gb300 import _abi
+    from watercube_gb300.fluid import dam_break_params, finalize, generate_dam_break
+
+    _abi.check(_abi.lib().wc_set_device(0), "select device")
+    n, dt, desc = WORKLOADS["dam1m"]
+    p = finalize(dam_break_params(n))
+    st = generate_dam_break(p, 0)
+    with Clocks(0) as clocks:
+        r = run_rollouts(p, st, dt, args.steps)
+    line = {
+        "metric": "particle-steps/s at 1M particles, surrogate-assisted rollout (K=4, 1% density tolerance)",
+        "value": r["surrogate"]["particle_steps_per_s"],
+        "unit": UNIT,
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": r["surrogate"]["ms_device"] / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 solver, bf16 network (fp32 accumulate)",
+        "data": "synthetic",
+        "config": {"workload": desc + ", rollout from the initial state", "particles": n, "dt": dt},
+        "rollout": r,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_ours(args):
     rank, world, local, reduce_max, barrier = dist_setup(args.gpus)
     from watercube_gb300 import _abi
@@ -357,6 +429,8 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(p, st, dt, os.cpu_count() or 1)
+    if rank == 0 and world == 1 and not args.no_rollout and args.workload == "dam1m":
+        line["rollout"] = run_rollouts(p, st, dt, args.rollout_steps)
     f.close()
     hin.free()
     hout.free()
@@ -418,8 +492,10 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512"], default="dam1m")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512", "rollout1m"], default="dam1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-rollout", action="store_true")
+    ap.add_argument("--rollout-steps", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -427,6 +503,8 @@ def main():
         return run_reference(args)
     if args.workload == "batch512":
         return run_batch(args)
+    if args.workload == "rollout1m":
+        return run_rollout_workload(args)
     return run_ours(args)
 
 

@@ -319,6 +319,34 @@ WC_API wc_status wc_batch_tune(wc_batch* b, float dt, wc_tuning* out);
 WC_API wc_status wc_batch_set_tuning(wc_batch* b, const wc_tuning* t);
 WC_API wc_status wc_batch_get_tuning(const wc_batch* b, wc_tuning* out);
 
+/* ---- snapshots ---------------------------------------------------------------------------- */
+/*
+ * No counterpart in the reference (Fluid::reset is a no-op, Fluid.h:57). A snapshot holds a
+ * fluid's state buffer (SoA float4 position+density and velocity+pressure, in the order of the
+ * last sort), its particle ids when tracked, the step count and the parameters (with the
+ * gravity and mouse ray in effect), followed by an FNV-1a 64 checksum of all preceding bytes.
+ * A fluid loaded from a snapshot continues bit for bit.
+ */
+typedef struct wc_snapshot_header {
+    char magic[8];          /* "WCSNAP\0\1" */
+    uint32_t version;       /* 1 */
+    uint32_t header_bytes;  /* sizeof(wc_snapshot_header) */
+    uint64_t num_particles;
+    uint64_t step;          /* wc_fluid_step_count when saved */
+    uint64_t seed;          /* the caller's seed of the initial state, informational */
+    uint32_t has_ids;       /* 1: uint32 ids[n] follow the two float4 arrays */
+    uint32_t reserved;
+    wc_params params;
+} wc_snapshot_header;
+
+WC_API wc_status wc_fluid_save_snapshot(wc_fluid* f, const char* path, uint64_t seed);
+/* Reads and verifies a snapshot (magic, version, sizes, checksum); fills the header. */
+WC_API wc_status wc_snapshot_read_header(const char* path, wc_snapshot_header* out);
+/* Load into a fluid created with the same parameters (gravity and mouse ray excepted: they are
+   taken from the snapshot). */
+WC_API wc_status wc_fluid_load_snapshot(wc_fluid* f, const char* path);
+WC_API wc_status wc_fluid_create_from_snapshot(const char* path, wc_fluid** out);
+
 /* ---- learned surrogate: network operations ---------------------------------------------- */
 /*
  * No counterpart in the reference. Building blocks of the message-passing surrogate; all

@@ -1,0 +1,79 @@
+"""What the trained network gains over the method without it.
+
+The method without the network reuses the last SPH acceleration for the skipped steps of a
+judged rollout (WC_ROLLOUT_STALE): with an SPH judge every K steps, a skipped step's
+acceleration is 1 .. K-1 steps old. The network predicts the current step's acceleration from
+the current state instead. On scenes it was not trained on (a different scene draw than the
+committed weights' training set), its mean per-step error must be below the stale method's at
+K = 8, and the rollouts of both stay finite and inside the box. The per-step comparison at K = 4
+and the trajectory errors are reported in the assertion messages, not asserted: in closed loop
+the network's own errors feed its velocity-history features and its trajectory drifts further
+from plain SPH than the stale method's.
+"""
+import numpy as np
+import pytest
+
+from watercube_gb300 import _abi
+from watercube_gb300.batch import batch_specs
+from watercube_gb300.fluid import Fluid
+from watercube_gb300.surrogate import WC_ROLLOUT_SPH, WC_ROLLOUT_STALE, WC_ROLLOUT_SURROGATE, Trainer, record_samples, rollout
+from watercube_gb300.train_surrogate import DEFAULT_WEIGHTS, load_weights, rel_error, stale_errors
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def trained(gpu):
+    if not DEFAULT_WEIGHTS.is_file():
+        pytest.fail(f"trained weights missing: {DEFAULT_WEIGHTS}")
+    s = load_weights()
+    yield s
+    s.close()
+
+
+@pytest.fixture(scope="module")
+def held_out(gpu):
+    specs = batch_specs(6, 2048, 8192, seed=7)  # the committed weights were trained on seed 1
+    params, samples = record_samples(specs, steps=24, dt=1e-3, every=1, start=0)
+    by = {(x.scene, x.step): x for x in samples}
+    return params, samples, by
+
+
+def test_network_beats_stale_acceleration_per_step(trained, held_out):
+    params, samples, by = held_out
+    evals = [x for x in samples if x.step >= 8][::3]
+    t = Trainer(trained, params)
+    try:
+        net = float(np.mean([rel_error(t.predict(x), x.target) for x in evals]))
+    finally:
+        t.close()
+    stale = stale_errors(evals, by, 7)
+    k4 = float(np.mean([stale[k] for k in range(1, 4)]))
+    k8 = float(np.mean([stale[k] for k in range(1, 8)]))
+    msg = f"network {net:.4f}, stale K=4 {k4:.4f}, stale K=8 {k8:.4f}, stale by age {stale}"
+    assert net < k8, msg
+    assert net < 0.5, msg  # far better than gravity alone (about 0.75 on these scenes)
+
+
+def test_rollouts_against_plain_sph(trained, held_out):
+    params, samples, by = held_out
+    report = []
+    for sc in (0, 3):
+        x = by[(sc, 8)]
+        p = params[sc].copy()
+        p.flags |= _abi.WC_FLAG_TRACK_IDS
+        res = {}
+        for mode, name in ((WC_ROLLOUT_SPH, "plain"), (WC_ROLLOUT_SURROGATE, "surrogate"), (WC_ROLLOUT_STALE, "stale")):
+            with Fluid("g", p) as f:
+                f.setup(x.state)
+                st = rollout(f, x.dt, 16, 4, 1e9, mode, trained, x.hist)
+                out, ids = f.particles(), f.particle_ids()
+            pos = np.empty((len(ids), 3))
+            pos[ids] = out["position"]
+            assert np.all(np.isfinite(pos)) and np.all((pos >= 0) & (pos <= p.size))
+            assert st["diag_end"][0] == st["diag_start"][0]
+            res[name] = pos
+        h = p.kernel_radius
+        report.append({k: float(np.sqrt(((res[k] - res["plain"]) ** 2).sum(1).mean()) / h) for k in ("surrogate", "stale")})
+    # reported, not asserted (see the module docstring)
+    assert all(np.isfinite(r["surrogate"]) and np.isfinite(r["stale"]) for r in report), report

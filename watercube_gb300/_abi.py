@@ -149,6 +149,20 @@ class GemmDesc(C.Structure):
     ]
 
 
+class SnapshotHeader(C.Structure):
+    _fields_ = [
+        ("magic", C.c_char * 8),
+        ("version", C.c_uint32),
+        ("header_bytes", C.c_uint32),
+        ("num_particles", C.c_uint64),
+        ("step", C.c_uint64),
+        ("seed", C.c_uint64),
+        ("has_ids", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("params", Params),
+    ]
+
+
 class SurrogateConfig(C.Structure):
     _fields_ = [
         ("layers", C.c_uint32),
@@ -243,6 +257,10 @@ def _declare(lib) -> None:
         "wc_batch_set_tuning": (S, [P, C.POINTER(Tuning)]),
         "wc_batch_get_tuning": (S, [P, C.POINTER(Tuning)]),
         "wc_nn_gemm": (S, [C.POINTER(GemmDesc), P, P]),
+        "wc_fluid_save_snapshot": (S, [P, C.c_char_p, C.c_uint64]),
+        "wc_snapshot_read_header": (S, [C.c_char_p, C.POINTER(SnapshotHeader)]),
+        "wc_fluid_load_snapshot": (S, [P, C.c_char_p]),
+        "wc_fluid_create_from_snapshot": (S, [C.c_char_p, C.POINTER(P)]),
         "wc_surrogate_config_default": (None, [C.POINTER(SurrogateConfig)]),
         "wc_surrogate_create": (S, [C.POINTER(SurrogateConfig), C.POINTER(P)]),
         "wc_surrogate_destroy": (None, [P]),

@@ -30,12 +30,6 @@ using namespace wc;
 
 namespace {
 
-#define WC_TRY(expr)                \
-    do {                            \
-        wc_status s_ = (expr);      \
-        if (s_ != WC_OK) return s_; \
-    } while (0)
-
 template <class T>
 wc_status dalloc(T** p, size_t count) {
     *p = nullptr;

@@ -58,12 +58,6 @@ wc_status dalloc(T** p, size_t count) {
     return WC_OK;
 }
 
-#define WC_TRY(expr)                          \
-    do {                                      \
-        wc_status s_ = (expr);                \
-        if (s_ != WC_OK) return s_;           \
-    } while (0)
-
 void free_all(wc_fluid* f) {
     DevBuffers& d = f->d;
     void* ptrs[] = {d.pos_a,     d.vel_a,        d.pos_b,     d.vel_b,    d.ids_a,           d.ids_b,
@@ -244,11 +238,16 @@ FluidInternals fluid_internals(wc_fluid* f) {
 void fluid_enqueue_sort(wc_fluid* f) { enqueue_sort(f); }
 
 wc_status fluid_graph_step(wc_fluid* f, float dt) {
+    // the caller counts its own steps (a judged rollout step runs this and a candidate)
+    const uint64_t steps = f->steps;
     f->in.dt = dt;
-    return launch_step(f, f->in);
+    const wc_status rc = launch_step(f, f->in);
+    f->steps = steps;
+    return rc;
 }
 
 void fluid_count_step(wc_fluid* f) { ++f->steps; }
+void fluid_set_step_count(wc_fluid* f, uint64_t steps) { f->steps = steps; }
 
 }  // namespace wc
 

@@ -169,6 +169,7 @@ FluidInternals fluid_internals(wc_fluid* f);
 void fluid_enqueue_sort(wc_fluid* f);
 wc_status fluid_graph_step(wc_fluid* f, float dt);  // one plain SPH step (graph replay)
 void fluid_count_step(wc_fluid* f);
+void fluid_set_step_count(wc_fluid* f, uint64_t steps);
 
 SceneConsts make_scene_consts(const wc_params& p);
 StepInputs make_step_inputs(const wc_params& p, float dt);

@@ -36,12 +36,6 @@ using namespace wc::nn;
 
 namespace {
 
-#define WC_TRY(expr)                \
-    do {                            \
-        wc_status s_ = (expr);      \
-        if (s_ != WC_OK) return s_; \
-    } while (0)
-
 constexpr uint32_t W = 128;  // latent width
 constexpr uint32_t NODE_IN = 32, EDGE_IN = 16, OUT = 16;
 constexpr size_t NONE = ~size_t(0);

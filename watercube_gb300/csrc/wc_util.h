@@ -20,3 +20,10 @@ const char* last_error();
             return ::wc::fail(e_ == cudaErrorMemoryAllocation ? WC_ERR_OOM : WC_ERR_CUDA,        \
                               "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
+
+// Return a non-OK status from the enclosing function.
+#define WC_TRY(expr)                \
+    do {                            \
+        wc_status s_ = (expr);      \
+        if (s_ != WC_OK) return s_; \
+    } while (0)

@@ -273,6 +273,22 @@ class Fluid:
         return [lib().wc_step_kernel_name(i).decode() for i in range(lib().wc_step_kernel_count())]
 
     # ---- teardown -------------------------------------------------------------------------------
+    # ---- snapshots (no counterpart in the reference) -------------------------------------------
+    def save_snapshot(self, path, seed: int = 0) -> None:
+        check(lib().wc_fluid_save_snapshot(self._require(), str(path).encode(), int(seed)), "wc_fluid_save_snapshot")
+
+    def load_snapshot(self, path) -> None:
+        check(lib().wc_fluid_load_snapshot(self._require(), str(path).encode()), "wc_fluid_load_snapshot")
+
+    @staticmethod
+    def from_snapshot(path, name: str = "fluid") -> "Fluid":
+        hdr = snapshot_header(path)
+        f = Fluid(name, hdr.params)
+        h = C.c_void_p()
+        check(lib().wc_fluid_create_from_snapshot(str(path).encode(), C.byref(h)), "wc_fluid_create_from_snapshot")
+        f._handle = h
+        return f
+
     def close(self) -> None:
         if self._handle is not None:
             lib().wc_fluid_destroy(self._handle)
@@ -319,3 +335,10 @@ class PinnedBuffer:
             self.free()
         except Exception:
             pass
+
+
+def snapshot_header(path) -> A.SnapshotHeader:
+    """The verified header of a snapshot file (magic, version, sizes and checksum checked)."""
+    h = A.SnapshotHeader()
+    check(lib().wc_snapshot_read_header(str(path).encode(), C.byref(h)), "wc_snapshot_read_header")
+    return h

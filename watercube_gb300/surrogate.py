@@ -146,10 +146,12 @@ class Sample:
     target: np.ndarray  # (n, 4) SPH acceleration of the state (w = 0)
 
 
-def record_samples(specs, steps: int, dt: float, every: int = 1, start: int = 0) -> tuple[list, list[Sample]]:
+def record_samples(specs, steps: int, dt: float, every: int = 1, start: int = 0, sink=None,
+                   keep: bool = True) -> tuple[list, list[Sample]]:
     """Run the batched solver on `specs` for `steps` steps with acceleration recording on and
     collect one Sample per scene every `every` steps from step `start`. Returns (params per
-    scene, samples)."""
+    scene, samples). `sink` (a DatasetWriter, or anything with write(Sample)) receives every
+    sample as it is made; keep=False then holds none in memory."""
     params = [scene_params(s) for s in specs]
     initial = [scene_particles(s, p) for s, p in zip(specs, params)]
     samples: list[Sample] = []
@@ -175,8 +177,11 @@ def record_samples(specs, steps: int, dt: float, every: int = 1, start: int = 0)
             if t >= start and (t - start) % every == 0:
                 for s in range(len(specs)):
                     lo, hi = int(off[s]), int(off[s + 1])
-                    samples.append(Sample(s, t, dt, state_by_id[lo:hi].copy(), hist[:, lo:hi].copy(),
-                                          acc_by_id[lo:hi].copy()))
+                    smp = Sample(s, t, dt, state_by_id[lo:hi].copy(), hist[:, lo:hi].copy(), acc_by_id[lo:hi].copy())
+                    if sink is not None:
+                        sink.write(smp)
+                    if keep:
+                        samples.append(smp)
             state = b.particles()
             vel_by_id = np.zeros((total, 4), np.float32)
             vel_by_id[ids, :3] = state["velocity"]
