@@ -15,14 +15,17 @@
 // so every lane runs the same trip count. Partial sums are combined with shuffles in a fixed
 // order: results are deterministic.
 //
-// Density: the candidates' positions are staged in shared memory as x/y/z arrays and tested four
-// at a time (one 128-bit shared load per coordinate) with Blackwell's packed f32x2 arithmetic
-// (one instruction updates two candidates). Each lane records which of its candidates passed
-// as a bit string; the force pass replays exactly those bits, gathering four neighbours per
-// round, instead of testing all candidates again. Cells whose candidate
-// list does not fit the stage, cells of more than 32 particles and bit strings longer than the
-// per-particle slot take the direct path: the density pass reads candidates from global memory
-// and the force pass culls into a per-lane shared-memory list.
+// Density: the candidates' positions are staged in shared memory as x/y/z arrays by
+// asynchronous copies (cp.async: every row in flight at once, one wait) and tested four at a
+// time with Blackwell's packed f32x2 arithmetic (one 128-bit shared load yields two packed
+// pairs; one instruction updates two candidates). Each lane records which of its candidates
+// passed as a bit string. The force pass decodes those bits once per cell into one neighbour
+// list per target (shared memory, prefix sums over the target's slices), and the target's
+// slices then split its list evenly, gathering four neighbours per round, instead of testing
+// all candidates again. Cells whose candidate list does not fit the stage, cells of more than
+// 32 particles and bit strings longer than the per-particle slot take the direct path: the
+// density pass reads candidates from global memory and the force pass culls into per-lane
+// shared-memory lists.
 //
 // Neighbour test: |r| < h is evaluated exactly as sqrtf(fma(dz,dz,fma(dy,dy,dx*dx))) < h would
 // be, as d2 <= cull with cull = the largest float whose sqrtf is below h, so the neighbour
@@ -64,6 +67,30 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
 
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// Four staged candidates against one target: hit bits (bit c for candidate c) and the Poly6
+// weights (cull - d2)^3 of the hits added to acc01 / acc23.
+__device__ __forceinline__ uint32_t quad_hits(const ulonglong2* q, f2 px, f2 py, f2 pz, f2 cull2, f2& acc01,
+                                              f2& acc23) {
+    const ulonglong2 X = q[0], Y = q[STAGE_CAP / 4], Z = q[STAGE_CAP / 2];
+    const f2 dx01 = sub2(px, X.x), dx23 = sub2(px, X.y);
+    const f2 dy01 = sub2(py, Y.x), dy23 = sub2(py, Y.y);
+    const f2 dz01 = sub2(pz, Z.x), dz23 = sub2(pz, Z.y);
+    const f2 d01 = fma2(dz01, dz01, fma2(dy01, dy01, mul2(dx01, dx01)));
+    const f2 d23 = fma2(dz23, dz23, fma2(dy23, dy23, mul2(dx23, dx23)));
+    // u = cull - d2 >= 0 exactly when d2 <= cull (a tie gives +0): the sign bits are the misses.
+    float u0, u1, u2, u3;
+    upk(sub2(cull2, d01), u0, u1);
+    upk(sub2(cull2, d23), u2, u3);
+    const uint32_t miss = (__float_as_uint(u0) >> 31) | ((__float_as_uint(u1) >> 30) & 2u) |
+                          ((__float_as_uint(u2) >> 29) & 4u) | ((__float_as_uint(u3) >> 28) & 8u);
+    // Poly6 weight (cull - d2)^3 for hits, 0 otherwise (cull is h^2 to the ulp).
+    const f2 w01 = pk(fmaxf(u0, 0.f), fmaxf(u1, 0.f));
+    const f2 w23 = pk(fmaxf(u2, 0.f), fmaxf(u3, 0.f));
+    acc01 = fma2(mul2(w01, w01), w01, acc01);
+    acc23 = fma2(mul2(w23, w23), w23, acc23);
+    return miss ^ 0xFu;
 }
 
 // ---- per-cell geometry ------------------------------------------------------------------------
@@ -298,16 +325,19 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
         if (cr.total + pad <= (uint32_t)STAGE_CAP) {
             // Stage: the concatenated candidate list as x/y/z arrays, then `pad` far-away
             // entries (their d2 overflows to +inf, so they never pass).
-#pragma unroll 1
+            // Asynchronous copies (no registers, all rows in flight at once), one wait.
+            const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(sx);
+#pragma unroll
             for (int r = 0; r < 9; ++r) {
                 const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
                 const uint32_t len = __shfl_sync(FULL, cr.len, r);
                 const uint32_t base = __shfl_sync(FULL, cr.pex, r);
                 for (uint32_t j = lane; j < len; j += 32u) {
-                    const float4 v = __ldg(pos_in + lo + j);
-                    sx[base + j] = v.x;
-                    sy[base + j] = v.y;
-                    sz[base + j] = v.z;
+                    const float* g = reinterpret_cast<const float*>(pos_in + lo + j);
+                    const uint32_t a = s0 + 4u * (base + j);
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(g) : "memory");
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a + 4u * STAGE_CAP), "l"(g + 1) : "memory");
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a + 8u * STAGE_CAP), "l"(g + 2) : "memory");
                 }
             }
             for (uint32_t j = lane; j < pad; j += 32u) {
@@ -315,6 +345,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
                 sy[cr.total + j] = 1e30f;
                 sz[cr.total + j] = 1e30f;
             }
+            asm volatile("cp.async.wait_all;" ::: "memory");
             __syncwarp();
             const bool single = cr.cend - cr.cbeg <= 32u;
             for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
@@ -325,37 +356,22 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
                 const uint32_t ti = t0 + tm.t;
                 const float4 pi = pos_in[ti];
                 const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
-                // Quads are 16-byte aligned: q is a multiple of 4 floats.
-                const float4* bx = reinterpret_cast<const float4*>(sx) + tm.sl;
-                const float4* by = reinterpret_cast<const float4*>(sy) + tm.sl;
-                const float4* bz = reinterpret_cast<const float4*>(sz) + tm.sl;
-                f2 acc01 = pk(0.f, 0.f), acc23 = pk(0.f, 0.f);
-                uint32_t nh = 0, it = 0;
+                // Quads are 16-byte aligned (q is a multiple of 4 floats); one 128-bit load gives
+                // two packed pairs, the f32x2 operands as they are. y and z follow x in the stage.
+                const ulonglong2* qx = reinterpret_cast<const ulonglong2*>(sx) + tm.sl;
+                f2 acc01 = 0ull, acc23 = 0ull;  // +0.0f pairs
+                uint32_t nh = 0;
                 for (uint32_t w = 0; w < ms.nwords; ++w) {
                     uint32_t word = 0;
                     const uint32_t jend = min(8u, ms.IT - 8u * w);
-#pragma unroll 2
-                    for (uint32_t j = 0; j < jend; ++j, ++it) {
-                        const uint32_t qd = it * tm.S;
-                        const float4 X = bx[qd], Y = by[qd], Z = bz[qd];
-                        const f2 dx01 = sub2(px, pk(X.x, X.y)), dx23 = sub2(px, pk(X.z, X.w));
-                        const f2 dy01 = sub2(py, pk(Y.x, Y.y)), dy23 = sub2(py, pk(Y.z, Y.w));
-                        const f2 dz01 = sub2(pz, pk(Z.x, Z.y)), dz23 = sub2(pz, pk(Z.z, Z.w));
-                        const f2 d01 = fma2(dz01, dz01, fma2(dy01, dy01, mul2(dx01, dx01)));
-                        const f2 d23 = fma2(dz23, dz23, fma2(dy23, dy23, mul2(dx23, dx23)));
-                        // u = cull - d2 >= 0 exactly when d2 <= cull (a tie gives +0): the
-                        // sign bits are the misses.
-                        float u0, u1, u2, u3;
-                        upk(sub2(cull2, d01), u0, u1);
-                        upk(sub2(cull2, d23), u2, u3);
-                        const uint32_t miss = (__float_as_uint(u0) >> 31) | ((__float_as_uint(u1) >> 31) << 1) |
-                                              ((__float_as_uint(u2) >> 31) << 2) | ((__float_as_uint(u3) >> 31) << 3);
-                        word |= (~miss & 0xFu) << (4u * j);
-                        // Poly6 weight (cull - d2)^3 for hits, 0 otherwise (cull is h^2 to the ulp).
-                        const f2 w01 = pk(fmaxf(u0, 0.f), fmaxf(u1, 0.f));
-                        const f2 w23 = pk(fmaxf(u2, 0.f), fmaxf(u3, 0.f));
-                        acc01 = fma2(mul2(w01, w01), w01, acc01);
-                        acc23 = fma2(mul2(w23, w23), w23, acc23);
+                    if (jend == 8u) {
+#pragma unroll
+                        for (uint32_t j = 0; j < 8u; ++j, qx += tm.S)
+                            word |= quad_hits(qx, px, py, pz, cull2, acc01, acc23) << (4u * j);
+                    } else {
+#pragma unroll 1
+                        for (uint32_t j = 0; j < jend; ++j, qx += tm.S)
+                            word |= quad_hits(qx, px, py, pz, cull2, acc01, acc23) << (4u * j);
                     }
                     nh += __popc(word);
                     if (store) hits[(size_t)ti * MASK_WORDS + w * tm.S + tm.sl] = word;
@@ -485,7 +501,7 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
 }
 
 template <bool BATCHED>
-__global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts sc0, const BatchTables bt,
+__global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts sc0, const BatchTables bt,
                                                                const StepInputs in, const uint32_t n,
                                                                const uint32_t num_cells,
                                                                const float4* __restrict__ pos_b,
@@ -546,28 +562,60 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts
             const float4 pi = pos_b[ti];
             const float4 vi = vel_b[ti];
             float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (tm.active) {
-                for (uint32_t w = 0; w < ms.nwords; ++w) {
-                    uint32_t word = __ldg(hits + (size_t)ti * MASK_WORDS + w * tm.S + tm.sl);
-                    while (word) {
-                        // Four neighbours per round so their loads overlap; empty places take
-                        // the particle itself, whose terms are exactly zero.
+            // Each lane's hit count, its offset among its target's slices, the target's total,
+            // and the target's segment in the warp's neighbour list (targets in order).
+            uint32_t cnt = 0;
+            if (tm.active)
+                for (uint32_t w = 0; w < ms.nwords; ++w) cnt += __popc(__ldg(hits + (size_t)ti * MASK_WORDS + w * tm.S + tm.sl));
+            uint32_t inc = cnt;
+            for (uint32_t d = 1; d < tm.S; d <<= 1) {
+                const uint32_t v = __shfl_up_sync(FULL, inc, d * nt);
+                if (tm.sl >= d) inc += v;
+            }
+            const uint32_t T = __shfl_sync(FULL, inc, tm.t + (tm.S - 1u) * nt);
+            const uint32_t tv = lane < nt ? T : 0u;
+            uint32_t tinc = tv;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t v = __shfl_up_sync(FULL, tinc, d);
+                if ((int)lane >= d) tinc += v;
+            }
+            const uint32_t all = __shfl_sync(FULL, tinc, 31);
+            const uint32_t seg = __shfl_sync(FULL, tinc - tv, tm.t);
+            if (all <= (uint32_t)(FORCE_LIST_CAP * 32)) {
+                // Decode the bits once into the target's list segment ...
+                if (tm.active) {
+                    uint32_t at = seg + inc - cnt;
+                    const uint32_t s4 = 4u * tm.S;
+                    for (uint32_t w = 0; w < ms.nwords; ++w) {
+                        uint32_t word = __ldg(hits + (size_t)ti * MASK_WORDS + w * tm.S + tm.sl);
+                        const uint32_t qb = 4u * (8u * w * tm.S + tm.sl);
+                        while (word) {
+                            const uint32_t bit = (uint32_t)__ffs(word) - 1u;
+                            word &= word - 1u;
+                            const uint32_t q = qb + (bit >> 2) * s4 + (bit & 3u);
+                            // Bits always come from this step's density pass over the same
+                            // tables; the checks only keep a stage-by-stage caller's stale bits
+                            // in bounds (the particle itself contributes exactly zero).
+                            uint32_t s = ti;
+                            if (q < cr.total) {
+                                const uint32_t v = slot[q];
+                                if (v < n) s = v;
+                            }
+                            list[at++] = s;
+                        }
+                    }
+                }
+                __syncwarp();
+                // ... then the target's slices split its list evenly, four entries per round.
+                if (tm.active) {
+                    const uint32_t* lst = list + seg;
+                    for (uint32_t e = tm.sl; e < T; e += 4u * tm.S) {
                         uint32_t k[4];
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
-                            k[u] = ti;
-                            if (word) {
-                                const uint32_t b = (uint32_t)__ffs(word) - 1u;
-                                word &= word - 1u;
-                                const uint32_t q = 4u * ((8u * w + (b >> 2)) * tm.S + tm.sl) + (b & 3u);
-                                // Bits always come from this step's density pass over the same
-                                // tables; the checks only keep a stage-by-stage caller's stale
-                                // bits in bounds.
-                                if (q < cr.total) {
-                                    const uint32_t s = slot[q];
-                                    if (s < n) k[u] = s;
-                                }
-                            }
+                            const uint32_t ee = e + (uint32_t)u * tm.S;
+                            k[u] = ee < T ? lst[ee] : ti;
                         }
                         float4 pj[4], vj[4];
 #pragma unroll
@@ -577,6 +625,40 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_kernel(const SceneConsts
                         }
 #pragma unroll
                         for (int u = 0; u < 4; ++u) pair_terms(pi, vi, pj[u], vj[u], sc.h, f);
+                    }
+                }
+            } else if (tm.active) {
+                for (uint32_t w = 0; w < ms.nwords; ++w) {
+                    uint32_t word = __ldg(hits + (size_t)ti * MASK_WORDS + w * tm.S + tm.sl);
+                    const uint32_t qb = 4u * (8u * w * tm.S + tm.sl), s4 = 4u * tm.S;
+                    while (word) {
+                        // Two neighbours per round so their loads overlap; an empty place takes
+                        // the particle itself, whose terms are exactly zero.
+                        uint32_t k[2];
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            k[u] = ti;
+                            if (word) {
+                                const uint32_t b = (uint32_t)__ffs(word) - 1u;
+                                word &= word - 1u;
+                                const uint32_t q = qb + (b >> 2) * s4 + (b & 3u);
+                                // Bits always come from this step's density pass over the same
+                                // tables; the checks only keep a stage-by-stage caller's stale
+                                // bits in bounds.
+                                if (q < cr.total) {
+                                    const uint32_t s = slot[q];
+                                    if (s < n) k[u] = s;
+                                }
+                            }
+                        }
+                        float4 pj[2], vj[2];
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            pj[u] = __ldg(pos_b + k[u]);
+                            vj[u] = __ldg(vel_b + k[u]);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) pair_terms(pi, vi, pj[u], vj[u], sc.h, f);
                     }
                 }
             }
