@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
         }
         if (replay) {
             // Replay the density pass's bit strings: same team, same candidate numbering.
-#pragma unroll 1
+#pragma unroll
             for (int r = 0; r < 9; ++r) {
                 const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
                 const uint32_t len = __shfl_sync(FULL, cr.len, r);
