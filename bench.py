@@ -15,6 +15,8 @@ cpu_baseline  the CPU transcription of the reference's stages (oracle, FP32) on 
            cores, on a bounded sample of the same workload.
 --impl reference  times the reference's own shader code compiled for the host CPU
            (oracle/_ref, when built) or else the oracle's transcription, all threads.
+surface    surface extraction of the same state: colour field on 256^3 vertices and marching
+           cubes, CUDA-event times.
 rollout    the judged rollout at the same size from the same initial state (plain SPH, the
            learned surrogate with an SPH judge every K = 4 steps, and the stale-acceleration
            method without the network), a bounded number of steps each; `--workload rollout1m`
@@ -290,6 +292,28 @@ def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01) -> 
     return out
 
 
+def run_surface(p, st, grid_res: int = 256, reps: int = 5) -> dict:
+    """Surface extraction (colour field on grid_res^3 vertices + marching cubes) of the
+    workload's state, CUDA-event times of the field and of classify + scan + emit (median of
+    `reps` extractions after one warm-up)."""
+    from watercube_gb300.fluid import Fluid
+    from watercube_gb300.surface import Surface
+
+    with Fluid.create("surface", p) as f, Surface(grid_res, iso=0.5) as s:
+        f.setup(st)
+        s.extract(f)
+        fields, meshes = [], []
+        for _ in range(reps):
+            ntri = s.extract(f)
+            a, b = s.timings()
+            fields.append(a)
+            meshes.append(b)
+    V = grid_res**3
+    mf, mm = float(np.median(fields)), float(np.median(meshes))
+    return {"grid_res": grid_res, "triangles": ntri, "ms_field": mf, "ms_mesh": mm,
+            "vertices_per_s": V / (mf * 1e-3), "cubes_per_s": (grid_res - 1) ** 3 / (mm * 1e-3)}
+
+
 def run_rollout_workload(args):
     """--workload rollout1m: the judged rollouts at 1,048,576 particles from the dam break's initial
     state, --steps steps each (dt = 2.5e-4, K = 4, 1% density tolerance)."""
@@ -431,6 +455,7 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(p, st, dt, os.cpu_count() or 1)
     if rank == 0 and world == 1 and not args.no_rollout and args.workload == "dam1m":
         line["rollout"] = run_rollouts(p, st, dt, args.rollout_steps)
+        line["surface"] = run_surface(p, st)
     f.close()
     hin.free()
     hout.free()

@@ -347,6 +347,34 @@ WC_API wc_status wc_snapshot_read_header(const char* path, wc_snapshot_header* o
 WC_API wc_status wc_fluid_load_snapshot(wc_fluid* f, const char* path);
 WC_API wc_status wc_fluid_create_from_snapshot(const char* path, wc_fluid** out);
 
+/* ---- surface extraction ------------------------------------------------------------------ */
+/*
+ * No counterpart in the reference (it draws particles as points; surface reconstruction is its
+ * report's stated future work). A colour field phi(v) = sum_j (m / rho0) W_poly6(|v - x_j|, r)
+ * is evaluated on grid_res^3 vertices spanning [0, size]^3 (about 1 inside the fluid), and
+ * marching cubes extracts the iso-surface phi = iso as a triangle soup (9 floats per triangle,
+ * counter-clockwise seen from outside the fluid). Vertices shared by neighbouring cubes are
+ * bit-identical, so the mesh is watertight.
+ */
+typedef struct wc_surface wc_surface;
+typedef struct wc_surface_params {
+    uint32_t grid_res; /* vertices per axis, 2..1024 */
+    float iso;         /* iso-level of the colour field (0.5: half the rest density) */
+    float radius;      /* field kernel radius; 0 -> the fluid's h (at most the cell edge) */
+    uint32_t reserved;
+} wc_surface_params;
+
+WC_API wc_status wc_surface_create(const wc_surface_params* p, wc_surface** out);
+WC_API void wc_surface_destroy(wc_surface* s);
+/* Sort the fluid's current state, evaluate the field and build the mesh on the device. */
+WC_API wc_status wc_surface_extract(wc_surface* s, wc_fluid* f, uint64_t* num_triangles);
+WC_API wc_status wc_surface_get_triangles(wc_surface* s, float* out /* 9 x num_triangles */, uint64_t num_triangles);
+WC_API wc_status wc_surface_get_field(wc_surface* s, float* out /* grid_res^3, x fastest */, uint64_t count);
+/* CUDA-event times of the last extraction: field kernel, and classify + scan + emit. */
+WC_API wc_status wc_surface_timings(const wc_surface* s, float* ms_field, float* ms_mesh);
+/* The generated marching-cubes case table: counts[256], tris[256][36] (edge ids, -1 unused). */
+WC_API wc_status wc_surface_case_table(uint8_t* counts, int8_t* tris);
+
 /* ---- learned surrogate: network operations ---------------------------------------------- */
 /*
  * No counterpart in the reference. Building blocks of the message-passing surrogate; all

@@ -163,6 +163,10 @@ class SnapshotHeader(C.Structure):
     ]
 
 
+class SurfaceParams(C.Structure):
+    _fields_ = [("grid_res", C.c_uint32), ("iso", C.c_float), ("radius", C.c_float), ("reserved", C.c_uint32)]
+
+
 class SurrogateConfig(C.Structure):
     _fields_ = [
         ("layers", C.c_uint32),
@@ -261,6 +265,13 @@ def _declare(lib) -> None:
         "wc_snapshot_read_header": (S, [C.c_char_p, C.POINTER(SnapshotHeader)]),
         "wc_fluid_load_snapshot": (S, [P, C.c_char_p]),
         "wc_fluid_create_from_snapshot": (S, [C.c_char_p, C.POINTER(P)]),
+        "wc_surface_create": (S, [C.POINTER(SurfaceParams), C.POINTER(P)]),
+        "wc_surface_destroy": (None, [P]),
+        "wc_surface_extract": (S, [P, P, C.POINTER(C.c_uint64)]),
+        "wc_surface_get_triangles": (S, [P, P, C.c_uint64]),
+        "wc_surface_get_field": (S, [P, P, C.c_uint64]),
+        "wc_surface_timings": (S, [P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "wc_surface_case_table": (S, [P, P]),
         "wc_surrogate_config_default": (None, [C.POINTER(SurrogateConfig)]),
         "wc_surrogate_create": (S, [C.POINTER(SurrogateConfig), C.POINTER(P)]),
         "wc_surrogate_destroy": (None, [P]),
