@@ -65,7 +65,17 @@ enum {
     WC_FLAG_SPEED_CLAMP = 1u << 2,  /* per-component velocity clamp to +-max_speed (update.comp:5,199) */
     WC_FLAG_MOUSE_FORCE = 1u << 3,  /* repulsion from the mouse ray (update.comp:116-132) */
     WC_FLAG_TRACK_IDS = 1u << 4,    /* carry each particle's original index through every sort */
-    WC_FLAG_NEIGHBOR_COUNTS = 1u << 5 /* write per-particle neighbour counts in the density pass */
+    WC_FLAG_NEIGHBOR_COUNTS = 1u << 5, /* write per-particle neighbour counts in the density pass */
+    /* Boundary handling by wall weight functions (Harada et al. 2007), in closed form for a
+       continuous planar wall of rest density at each face of the box: a particle at distance
+       d < h from a wall gains rho0 * 315/256 * P(1 - d/h) of density, with
+       P(x) = x^5 (16/5 - 16x/3 + 24x^2/7 - x^3 + x^4/9) (half the kernel's mass at d = 0), which
+       enters the equation of state; and, when its pressure is positive, the mirrored pressure
+       push (p rho0 / rho) * (30/h) * (x^4/4 - x^5/5) away from the wall (the surface integral
+       of the Spiky kernel over the wall plane). No counterpart in the reference: the
+       replacement for its pseudo wall density and force that its report names as the next
+       physics fix. */
+    WC_FLAG_WALL_WEIGHTS = 1u << 6
 };
 
 /* The reference's four active behaviours. */

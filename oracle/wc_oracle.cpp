@@ -169,6 +169,36 @@ inline T wall_density(const Consts<T>& c, const T p[3]) {  // density.comp:57-79
     return d * T(4);
 }
 
+// Wall weight functions for a continuous planar wall (WC_FLAG_WALL_WEIGHTS; no counterpart in
+// the reference): density rho0 * 315/256 * P(x), x = 1 - d/h, P(x) = x^5 (16/5 - 16x/3 + 24x^2/7
+// - x^3 + x^4/9), and the pressure push (p rho0 / rho) (30/h) (x^4/4 - x^5/5) away from the wall.
+template <class T>
+inline T wall_x(const Consts<T>& c, T d) {
+    return gclamp(T(1) - d / c.h, T(0), T(1));
+}
+template <class T>
+inline T wall_weight_density(const Consts<T>& c, const T p[3]) {
+    T acc = T(0);
+    for (int a = 0; a < 3; ++a) {
+        for (int side = 0; side < 2; ++side) {
+            const T s = wall_x(c, side ? c.size - p[a] : p[a]);
+            const T poly = (((s / T(9) - T(1)) * s + T(24) / T(7)) * s - T(16) / T(3)) * s + T(16) / T(5);
+            acc += s * s * s * s * s * poly;
+        }
+    }
+    return c.rho0 * (T(315) / T(256)) * acc;
+}
+template <class T>
+inline void wall_weight_push(const Consts<T>& c, const T p[3], T rho, T pressure, T f[3]) {
+    f[0] = f[1] = f[2] = T(0);
+    if (!(pressure > T(0))) return;
+    const T k = pressure * c.rho0 / rho * (T(30) / c.h);
+    for (int a = 0; a < 3; ++a) {
+        const T lo = wall_x(c, p[a]), hi = wall_x(c, c.size - p[a]);
+        f[a] = k * (lo * lo * lo * lo * (T(0.25) - T(0.2) * lo) - hi * hi * hi * hi * (T(0.25) - T(0.2) * hi));
+    }
+}
+
 template <class T>
 int density_impl(const wc_params* p, Particle<T>* s, uint32_t n, const uint32_t* counts, const uint32_t* offsets,
                  uint32_t* ncount, int threads) {
@@ -200,6 +230,7 @@ int density_impl(const wc_params* p, Particle<T>* s, uint32_t n, const uint32_t*
                 ++nb;
             }
         }
+        if (c.flags & WC_FLAG_WALL_WEIGHTS) density = density + wall_weight_density(c, pi);
         T total = density;
         if (c.flags & WC_FLAG_WALL_DENSITY) total = density + wall_density(c, pi);
         T pressure;
@@ -311,6 +342,11 @@ int update_impl(const wc_params* p, const Particle<T>* in, Particle<T>* out, uin
                 const T wv = (c.h - dist) * c.cv;
                 for (int a = 0; a < 3; ++a) vf[a] = vf[a] + (c.m * ((pj.vel[a] - pi.vel[a]) / pj.density)) * wv;
             }
+        }
+        if (c.flags & WC_FLAG_WALL_WEIGHTS) {
+            T ww[3];
+            wall_weight_push(c, pi.pos, pi.density, pi.pressure, ww);
+            for (int a = 0; a < 3; ++a) ext[a] = ext[a] + ww[a];
         }
         if (c.flags & (WC_FLAG_MOUSE_FORCE | WC_FLAG_WALL_FORCE)) {
             T mf[3] = {T(0), T(0), T(0)}, wf[3] = {T(0), T(0), T(0)};

@@ -29,6 +29,11 @@ def case(name: str, extra_flags: int = 0):
         p.flags |= extra_flags
         p = finalize(p)
         return p, generate_dam_break(p, 0)
+    if name == "dam16k_walls":
+        p = dam_break_params(16384)
+        p.flags |= _abi.WC_FLAG_WALL_WEIGHTS | extra_flags
+        p = finalize(p)
+        return p, generate_dam_break(p, 0)
     if name == "refdefaults":
         p = reference_params()
         p.flags |= extra_flags

@@ -22,6 +22,7 @@ CASES = [
     ("dam16k", 30, 1e-3),
     ("refdefaults", 20, 2e-4),
     ("dam16k_refphysics", 10, 2e-4),
+    ("dam16k_walls", 30, 1e-3),
     ("dam1m", 4, 2.5e-4),
 ]
 
@@ -162,3 +163,43 @@ def test_reference_physics_tracks_oracle(gpu, oracle):
     err = np.abs(pg - po).max()
     assert err <= 1e-5 * float(p.kernel_radius), f"{err:.3e}"
     assert dt > 0
+
+
+def test_wall_weights_fill_the_density_deficit_at_the_walls(gpu):
+    """A resting block against the floor and two walls: without boundary handling the particles
+    within h of a wall miss part of their kernel's mass; with the wall weight functions their
+    density matches the interior's."""
+    out = {}
+    for flags in (0, _abi.WC_FLAG_WALL_WEIGHTS):
+        p, st = case("dam16k", flags | _abi.WC_FLAG_NEIGHBOR_COUNTS)
+        srt, _, _ = gpu_density(p, st)
+        pos, rho = srt["position"], srt["density"]
+        h = p.kernel_radius
+        near = (pos[:, 1] < 0.5 * h) & (pos[:, 0] > 2 * h) & (pos[:, 0] < 0.3) & (pos[:, 2] > 2 * h) & (pos[:, 2] < 0.3)
+        inner = (pos[:, 1] > 3 * h) & (pos[:, 1] < 0.6) & (pos[:, 0] > 2 * h) & (pos[:, 0] < 0.3) & \
+                (pos[:, 2] > 2 * h) & (pos[:, 2] < 0.3)
+        out[flags] = (float(np.median(rho[near])), float(np.median(rho[inner])))
+    floor0, inner0 = out[0]
+    floor1, inner1 = out[_abi.WC_FLAG_WALL_WEIGHTS]
+    assert inner1 == pytest.approx(inner0, rel=1e-6)  # the interior does not see the walls
+    assert floor0 < 0.85 * inner0  # 0.81 on this lattice (the oracle's FP32 path)
+    assert floor1 == pytest.approx(inner1, rel=0.05)  # 1.02
+
+
+def test_wall_weights_keep_particles_off_the_walls(gpu):
+    """300 steps of the 16,384-particle dam break: with the wall weight functions the fluid stays
+    inside the box and fewer particles end on the clamp border (0.152 against 0.210 in the FP32
+    oracle's run of the same steps; the dam-break stiffness k = 3 is soft, so the falling column
+    reaches the floor in both)."""
+    frac = {}
+    for flags in (0, _abi.WC_FLAG_WALL_WEIGHTS):
+        p, st = case("dam16k", flags)
+        with fluid(p, st) as f:
+            f.step(1e-3, 300)
+            pos = f.particles()["position"]
+        assert np.all(np.isfinite(pos))
+        assert np.all((pos >= p.wall_border) & (pos <= p.size - p.wall_border))
+        b = np.float32(p.wall_border)
+        on = (pos == b) | (pos == np.float32(p.size) - b)
+        frac[flags] = on.any(axis=1).mean()
+    assert frac[_abi.WC_FLAG_WALL_WEIGHTS] < 0.85 * frac[0], frac

@@ -34,6 +34,7 @@ WC_FLAG_SPEED_CLAMP = 1 << 2
 WC_FLAG_MOUSE_FORCE = 1 << 3
 WC_FLAG_TRACK_IDS = 1 << 4
 WC_FLAG_NEIGHBOR_COUNTS = 1 << 5
+WC_FLAG_WALL_WEIGHTS = 1 << 6
 WC_FLAGS_REFERENCE = WC_FLAG_WALL_DENSITY | WC_FLAG_WALL_FORCE | WC_FLAG_SPEED_CLAMP | WC_FLAG_MOUSE_FORCE
 
 WC_BUFFER_STATE = 1

@@ -262,10 +262,42 @@ __device__ void mouse_force(const SceneConsts& c, const StepInputs& in, const fl
     for (int a = 0; a < 3; ++a) f[a] = (k * ((s * (tm[a] / dd)) * c.cs));
 }
 
+// Wall weight functions for a continuous planar wall (WC_FLAG_WALL_WEIGHTS): the density a
+// particle at distance d < h gains from one wall, rho0 * 315/256 * P(x) with x = 1 - d/h and
+// P(x) = x^5 (16/5 - 16x/3 + 24x^2/7 - x^3 + x^4/9), and the magnitude of the mirrored pressure
+// push per unit p rho0 / rho, (30/h) (x^4/4 - x^5/5).
+__device__ __forceinline__ float wall_x(float d, float h) { return fminf(fmaxf(1.f - d / h, 0.f), 1.f); }
+__device__ __forceinline__ float wall_weight_density(const SceneConsts& c, float x, float y, float z) {
+    const float d[6] = {x, c.size - x, y, c.size - y, z, c.size - z};
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float s = wall_x(d[k], c.h);
+        const float poly = (((s * (1.f / 9.f) - 1.f) * s + 24.f / 7.f) * s - 16.f / 3.f) * s + 16.f / 5.f;
+        const float s2 = s * s;
+        acc += s2 * s2 * s * poly;
+    }
+    return c.rho0 * (315.f / 256.f) * acc;
+}
+__device__ __forceinline__ void wall_weight_push(const SceneConsts& c, const float p[3], float rho, float pressure,
+                                                 float f[3]) {
+    f[0] = f[1] = f[2] = 0.f;
+    if (!(pressure > 0.f)) return;
+    const float k = pressure * c.rho0 / rho * (30.f / c.h);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float lo = wall_x(p[a], c.h), hi = wall_x(c.size - p[a], c.h);
+        const float w_lo = lo * lo * lo * lo * (0.25f - 0.2f * lo);
+        const float w_hi = hi * hi * hi * hi * (0.25f - 0.2f * hi);
+        f[a] = k * (w_lo - w_hi);  // away from the x = 0 wall, away from the x = size wall
+    }
+}
+
 __device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, uint32_t hits, const float4& pi,
                                               uint32_t ti, float* rho_out, float* p_out, uint32_t* ncount) {
     // The sum includes the particle itself (w = h^2): the reference's m*W(0) term.
-    const float rho = (sc.m * sc.c6) * sum;
+    float rho = (sc.m * sc.c6) * sum;
+    if (sc.flags & WC_FLAG_WALL_WEIGHTS) rho += wall_weight_density(sc, pi.x, pi.y, pi.z);
     float pressure;
     if (sc.eos == WC_EOS_LINEAR) {
         pressure = sc.p0 + sc.k * (rho - sc.rho0);
@@ -467,6 +499,12 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     const float rho = pi.w, pressure = vi.w;
     const float p3[3] = {pi.x, pi.y, pi.z};
     float ext[3] = {in.g[0] * rho, in.g[1] * rho, in.g[2] * rho};
+    if (sc.flags & WC_FLAG_WALL_WEIGHTS) {
+        float ww[3];
+        wall_weight_push(sc, p3, rho, pressure, ww);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) ext[a] += ww[a];
+    }
     if (sc.flags & (WC_FLAG_WALL_FORCE | WC_FLAG_MOUSE_FORCE)) {
         float wf[3] = {0.f, 0.f, 0.f}, mf[3] = {0.f, 0.f, 0.f};
         if (sc.flags & WC_FLAG_WALL_FORCE) wall_forces(sc, p3, wf);
