@@ -125,3 +125,54 @@ def test_wrong_sizes_rejected(gpu):
     with pytest.raises(_abi.WatercubeError):
         f.setup(states(np.full((9, 3), 0.5)))
     f.close()
+
+
+def crowd(n, p, seed=4):
+    """n particles inside one cell of p's grid (cell (10, 10, 10))."""
+    rng = np.random.default_rng(seed)
+    b = float(p.bin_size)
+    return states(10 * b + rng.uniform(0.1 * b, 0.9 * b, size=(n, 3)))
+
+
+def test_overfull_cell_is_not_evaluated(gpu):
+    """A cell of 3,000 particles (over the 2,048 limit; 2,000 is evaluated above): the neighbour
+    passes skip it, the particles keep their state, and the step reports WC_ERR_NUMERIC instead
+    of spending O(N^2) work on it. (Even unguarded this case would take well under a second.)"""
+    p = small(3000)
+    st = crowd(3000, p)
+    with fluid(p, st) as f:
+        f.step(1e-3, 3)
+        with pytest.raises(_abi.WatercubeError) as e:
+            f.synchronize()
+        assert e.value.status == _abi.WC_ERR_NUMERIC and "2048" in str(e.value)
+        out = f.particles()
+    assert np.array_equal(np.sort(out["position"], axis=0), np.sort(st["position"], axis=0))
+
+
+def test_nonfinite_state_is_bounded(gpu):
+    """Every position NaN: all particles bin to cell 0; the step reports the non-finite input and
+    the overfull cell without evaluating it."""
+    p = small(3000)
+    st = states(np.full((3000, 3), np.nan))
+    with fluid(p, st) as f:
+        f.step(1e-3, 5)
+        with pytest.raises(_abi.WatercubeError) as e:
+            f.synchronize()
+        assert e.value.status == _abi.WC_ERR_NUMERIC
+
+
+def test_overfull_rows_refused_by_surface_and_surrogate(gpu):
+    from watercube_gb300.surface import Surface
+    from watercube_gb300.surrogate import Surrogate
+
+    n = 7000  # a row of more than 3 x 2,048 particles
+    p = small(n)
+    st = crowd(n, p)
+    with fluid(p, st) as f, Surface(24) as s:
+        with pytest.raises(_abi.WatercubeError) as e:
+            s.extract(f)
+        assert e.value.status == _abi.WC_ERR_NUMERIC
+    with fluid(p, st) as f, Surrogate(layers=1) as sg:
+        with pytest.raises(_abi.WatercubeError) as e:
+            sg.sample(f, 1e-3, np.zeros((5, n, 4), np.float32))
+        assert e.value.status == _abi.WC_ERR_NUMERIC

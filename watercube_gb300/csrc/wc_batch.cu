@@ -250,6 +250,7 @@ wc_status capture(wc_batch* b, const StepInputs& in) {
     a.num_nonempty = b->d.num_nonempty;
     a.hits = b->d.hits;
     a.accel = b->d.accel;
+    a.err = b->d.err;
     a.bind();
     b->graph_in = in;
     return WC_OK;
@@ -279,6 +280,9 @@ wc_status read_errors(wc_batch* b) {
         WC_CUDA_TRY(cudaMemsetAsync(b->d.err, 0, sizeof(uint32_t), b->stream));
         WC_CUDA_TRY(cudaStreamSynchronize(b->stream));
         if (e & DEVERR_SCAN_TIMEOUT) return fail(WC_ERR_TIMEOUT, "cell scan look-back exceeded its wait limit");
+        if (e & DEVERR_CELL_OVERFLOW)
+            return fail(WC_ERR_NUMERIC, "a cell held more than %u particles (a collapsed or non-finite state); its "
+                                        "particles were not evaluated", MAX_CELL_PARTICLES);
         return fail(WC_ERR_NUMERIC, "a particle position was NaN or infinite when it was binned");
     }
     return WC_OK;

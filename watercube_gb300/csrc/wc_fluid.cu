@@ -185,6 +185,7 @@ wc_status capture_graph(wc_fluid* f, const StepInputs& in) {
     a.num_nonempty = f->d.num_nonempty;
     a.hits = f->d.hits;
     a.accel = f->d.accel;
+    a.err = f->d.err;
     a.bind();
     f->graph_in = in;
     return WC_OK;
@@ -216,6 +217,9 @@ wc_status read_device_errors(wc_fluid* f) {
         WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
         if (e & DEVERR_SCAN_TIMEOUT)
             return fail(WC_ERR_TIMEOUT, "cell scan look-back exceeded its wait limit; tables of that step are invalid");
+        if (e & DEVERR_CELL_OVERFLOW)
+            return fail(WC_ERR_NUMERIC, "a cell held more than %u particles (a collapsed or non-finite state); its "
+                                        "particles were not evaluated", MAX_CELL_PARTICLES);
         return fail(WC_ERR_NUMERIC, "a particle position was NaN or infinite when it was binned");
     }
     return WC_OK;

@@ -13,8 +13,15 @@ namespace wc {
 enum : uint32_t {
     DEVERR_NONFINITE = 1u << 0,    // a non-finite position was binned
     DEVERR_SCAN_TIMEOUT = 1u << 1,  // a scan tile gave up waiting on its predecessor
-    DEVERR_MMA_TIMEOUT = 1u << 2    // a tensor-core GEMM gave up waiting on its MMAs
+    DEVERR_MMA_TIMEOUT = 1u << 2,   // a tensor-core GEMM gave up waiting on its MMAs
+    DEVERR_CELL_OVERFLOW = 1u << 3  // a cell held more than MAX_CELL_PARTICLES particles
 };
+
+// Cells holding more particles than this (256 times the rest density's ~8 per cell) are not
+// evaluated: their particles get NaN density and keep their state, and the step reports
+// WC_ERR_NUMERIC. Such a cell only arises from a collapsed or non-finite state (every NaN
+// position bins to cell 0), where evaluating it would cost O(N^2) work per step.
+constexpr uint32_t MAX_CELL_PARTICLES = 2048;
 
 // Constants of one scene, by value in kernel parameters (single scene) or in a device table
 // (batched scenes).
@@ -143,11 +150,12 @@ struct ForceKernelArgs {
     const uint32_t* num_nonempty;
     const uint32_t* hits;
     float4* accel;
-    void* ptrs[16];
+    uint32_t* err;
+    void* ptrs[17];
     void bind() {
-        void* p[16] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b,
-                       &pos_a, &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits,  &accel};
-        for (int i = 0; i < 16; ++i) ptrs[i] = p[i];
+        void* p[17] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b, &pos_a,
+                       &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits, &accel, &err};
+        for (int i = 0; i < 17; ++i) ptrs[i] = p[i];
     }
 };
 

@@ -50,7 +50,7 @@ struct DevBuffers;
 namespace nn {
 
 void graph_count(const float4* pos, uint32_t n, const uint32_t* start, float bin, int32_t R, float cull,
-                 uint32_t* count, cudaStream_t s);
+                 uint32_t* count, uint32_t* err, cudaStream_t s);
 void graph_fill(const float4* pos, uint32_t n, const uint32_t* start, float bin, int32_t R, float cull,
                 const uint32_t* rowptr, uint32_t* col, cudaStream_t s);
 void graph_rev(uint32_t n, const uint32_t* rowptr, const uint32_t* col, uint32_t* recv, uint32_t* rev, cudaStream_t s);

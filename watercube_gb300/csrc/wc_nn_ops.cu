@@ -41,7 +41,8 @@ __device__ __forceinline__ int32_t cell_axis(float q, int32_t R) {
 template <int MODE>
 __global__ void graph_kernel(const float4* __restrict__ pos, uint32_t n, const uint32_t* __restrict__ start,
                              float bin, int32_t R, float cull, uint32_t* __restrict__ count,
-                             const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ col) {
+                             const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ col,
+                             uint32_t* __restrict__ err) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = pos[i];
@@ -56,7 +57,11 @@ __global__ void graph_kernel(const float4* __restrict__ pos, uint32_t n, const u
             if (y < 0 || y >= R) continue;
             const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < R ? cx + 1 : R - 1;
             const uint32_t row = (uint32_t)((z * R + y) * R);
-            const uint32_t lo = start[row + x0], hi = min(start[row + x1 + 1], n);
+            const uint32_t hi = min(start[row + x1 + 1], n), lo = min(start[row + x0], hi);
+            if (hi - lo > 3u * MAX_CELL_PARTICLES) {  // a collapsed state: no edges, reported
+                if (!MODE) atomicOr(err, DEVERR_CELL_OVERFLOW);
+                continue;
+            }
             for (uint32_t k = lo; k < hi; ++k) {
                 if (k == i) continue;
                 const float4 q = __ldg(pos + k);
@@ -419,12 +424,12 @@ inline unsigned blocks_for(size_t n, unsigned t) { return (unsigned)((n + t - 1)
 }  // namespace
 
 void graph_count(const float4* pos, uint32_t n, const uint32_t* start, float bin, int32_t R, float cull,
-                 uint32_t* count, cudaStream_t s) {
-    if (n) graph_kernel<0><<<blocks_for(n, 128), 128, 0, s>>>(pos, n, start, bin, R, cull, count, nullptr, nullptr);
+                 uint32_t* count, uint32_t* err, cudaStream_t s) {
+    if (n) graph_kernel<0><<<blocks_for(n, 128), 128, 0, s>>>(pos, n, start, bin, R, cull, count, nullptr, nullptr, err);
 }
 void graph_fill(const float4* pos, uint32_t n, const uint32_t* start, float bin, int32_t R, float cull,
                 const uint32_t* rowptr, uint32_t* col, cudaStream_t s) {
-    if (n) graph_kernel<1><<<blocks_for(n, 128), 128, 0, s>>>(pos, n, start, bin, R, cull, nullptr, rowptr, col);
+    if (n) graph_kernel<1><<<blocks_for(n, 128), 128, 0, s>>>(pos, n, start, bin, R, cull, nullptr, rowptr, col, nullptr);
 }
 void graph_rev(uint32_t n, const uint32_t* rowptr, const uint32_t* col, uint32_t* recv, uint32_t* rev, cudaStream_t s) {
     if (n) graph_rev_kernel<<<blocks_for(n, 128), 128, 0, s>>>(n, rowptr, col, recv, rev);

@@ -326,7 +326,8 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
                                                                  const uint32_t* __restrict__ cell_list,
                                                                  const uint32_t* __restrict__ num_nonempty,
                                                                  uint32_t* __restrict__ ncount,
-                                                                 uint32_t* __restrict__ hits) {
+                                                                 uint32_t* __restrict__ hits,
+                                                                 uint32_t* __restrict__ err) {
     __shared__ __align__(16) float s_stage[WARPS][3][STAGE_CAP];
     __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
     if (BATCHED) {
@@ -353,6 +354,16 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
         }
         const f2 cull2 = pk(sc.cull, sc.cull);
         const CellRows cr = cell_rows(start + coff, n, sc.R, cg - coff, lane);
+        if (cr.cend - cr.cbeg > MAX_CELL_PARTICLES) {
+            // not evaluated (see MAX_CELL_PARTICLES): NaN density and pressure, reported
+            for (uint32_t i = cr.cbeg + lane; i < cr.cend; i += 32u) {
+                rho_out[4 * (size_t)i] = __int_as_float(0x7fc00000);
+                p_out[4 * (size_t)i] = __int_as_float(0x7fc00000);
+                if (ncount) ncount[i] = 0u;
+            }
+            if (lane == 0 && err) atomicOr(err, DEVERR_CELL_OVERFLOW);
+            continue;
+        }
         const uint32_t pad = stage_padding(max_slices(cr.cend - cr.cbeg));
         if (cr.total + pad <= (uint32_t)STAGE_CAP) {
             // Stage: the concatenated candidate list as x/y/z arrays, then `pad` far-away
@@ -551,7 +562,8 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                                                                const uint32_t* __restrict__ cell_list,
                                                                const uint32_t* __restrict__ num_nonempty,
                                                                const uint32_t* __restrict__ hits,
-                                                               float4* __restrict__ accel) {
+                                                               float4* __restrict__ accel,
+                                                               uint32_t* __restrict__ err) {
     __shared__ uint32_t s_slot[WARPS][STAGE_CAP];             // candidate number -> sorted slot
     __shared__ uint32_t s_lists[WARPS][FORCE_LIST_CAP * 32];  // direct path: per-lane lists
     __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
@@ -578,6 +590,17 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
         }
         const CellRows cr = cell_rows(start + coff, n, sc.R, cg - coff, lane);
         const uint32_t ncell = cr.cend - cr.cbeg;
+        if (ncell > MAX_CELL_PARTICLES) {
+            // not evaluated (see MAX_CELL_PARTICLES): the particles keep their state, reported
+            for (uint32_t i = cr.cbeg + lane; i < cr.cend; i += 32u) {
+                pos_a[i] = pos_b[i];
+                vel_a[i] = vel_b[i];
+                if (ids_a) ids_a[i] = ids_b[i];
+                if (accel) accel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            if (lane == 0 && err) atomicOr(err, DEVERR_CELL_OVERFLOW);
+            continue;
+        }
         bool replay = false;
         if (ncell <= 32u && hits != nullptr) {
             const Team tm = make_team(ncell, lane);
@@ -779,27 +802,27 @@ void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims
     density_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
         sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
         reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty,
-        (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr, d.hits);
+        (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr, d.hits, d.err);
 }
 
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s) {
     force_kernel<false><<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, BatchTables{}, in, d.n, d.num_cells, d.pos_b,
                                                               d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
-                                                              d.cell_list, d.num_nonempty, d.hits, d.accel);
+                                                              d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
 }
 
 void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
     density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
         SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
-        reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits);
+        reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
 }
 
 void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
                           cudaStream_t s) {
     force_kernel<true><<<ld.grid_force, SPH_THREADS, 0, s>>>(SceneConsts{}, bt, in, d.n, d.num_cells, d.pos_b,
                                                              d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
-                                                             d.cell_list, d.num_nonempty, d.hits, d.accel);
+                                                             d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
 }
 
 const void* force_kernel_symbol(uint32_t) { return reinterpret_cast<const void*>(&force_kernel<false>); }

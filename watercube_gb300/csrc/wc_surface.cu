@@ -177,7 +177,8 @@ __device__ __forceinline__ float vcoord(uint32_t i, float spacing) { return __fm
 
 // phi at every vertex (x fastest). One thread per vertex.
 __global__ void field_kernel(Grid g, const float4* __restrict__ pos, uint32_t n, const uint32_t* __restrict__ start,
-                             float bin, int32_t R, float h2, float scale, float* __restrict__ phi) {
+                             float bin, int32_t R, float h2, float scale, float* __restrict__ phi,
+                             uint32_t* __restrict__ err) {
     const uint64_t V = (uint64_t)g.G * g.G * g.G;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t ix = (uint32_t)(v % g.G), iy = (uint32_t)((v / g.G) % g.G), iz = (uint32_t)(v / ((uint64_t)g.G * g.G));
@@ -198,7 +199,13 @@ __global__ void field_kernel(Grid g, const float4* __restrict__ pos, uint32_t n,
                 const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < R ? cx + 1 : R - 1;
                 const uint32_t row = (uint32_t)((z * R + y) * R);
                 const uint32_t hi = min(start[row + x1 + 1], n);
-                for (uint32_t k = min(start[row + x0], hi); k < hi; ++k) {
+                const uint32_t lo = min(start[row + x0], hi);
+                if (hi - lo > 3u * MAX_CELL_PARTICLES) {  // a collapsed state: not evaluated
+                    acc = __int_as_float(0x7fc00000);
+                    atomicOr(err, DEVERR_CELL_OVERFLOW);
+                    continue;
+                }
+                for (uint32_t k = lo; k < hi; ++k) {
                     const float4 q = __ldg(pos + k);
                     const float dx = __fsub_rn(px, q.x), dyy = __fsub_rn(py, q.y), dzz = __fsub_rn(pz, q.z);
                     const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dyy, dyy)), __fmul_rn(dzz, dzz));
@@ -394,7 +401,8 @@ WC_API wc_status wc_surface_extract(wc_surface* s, wc_fluid* f, uint64_t* num_tr
     cudaEventCreate(&e1);
     cudaEventCreate(&e2);
     cudaEventRecord(e0, fi.stream);
-    field_kernel<<<grid_blocks(V), 256, 0, fi.stream>>>(g, d.pos_b, d.n, d.start, sc.bin, sc.R, h2, scale, s->phi);
+    field_kernel<<<grid_blocks(V), 256, 0, fi.stream>>>(g, d.pos_b, d.n, d.start, sc.bin, sc.R, h2, scale, s->phi,
+                                                        s->err);
     cudaEventRecord(e1, fi.stream);
     classify_kernel<<<grid_blocks(cubes), 256, 0, fi.stream>>>(G, s->phi, s->p.iso, s->counts);
     DevBuffers sd{};
@@ -420,6 +428,9 @@ WC_API wc_status wc_surface_extract(wc_surface* s, wc_fluid* f, uint64_t* num_tr
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         cudaEventDestroy(e2);
+        if (err & DEVERR_CELL_OVERFLOW)
+            return fail(WC_ERR_NUMERIC, "a cell row held more than %u particles (a collapsed or non-finite state)",
+                        3u * MAX_CELL_PARTICLES);
         return fail(WC_ERR_TIMEOUT, "surface scan look-back exceeded its wait limit");
     }
     wc_status st = WC_OK;

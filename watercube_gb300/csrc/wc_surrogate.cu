@@ -401,7 +401,7 @@ wc_status build_graph(wc_surrogate* s, const FluidInternals& fi, uint32_t* e_out
     // The edge count is only known after the count pass: size the node side first.
     WC_TRY(ensure_work(s, n, std::max(s->work.cap_e, 1u), saved));
     Work& w = s->work;
-    graph_count(d.pos_b, n, d.start, sc.bin, sc.R, sc.cull, w.count, s->stream);
+    graph_count(d.pos_b, n, d.start, sc.bin, sc.R, sc.cull, w.count, s->d_err, s->stream);
     DevBuffers sd{};
     sd.n = n;
     sd.num_cells = n;
@@ -564,6 +564,9 @@ wc_status read_err(wc_surrogate* s) {
     WC_CUDA_TRY(cudaMemcpy(s->h_err, s->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     if (*s->h_err) {
         cudaMemset(s->d_err, 0, sizeof(uint32_t));
+        if (*s->h_err & DEVERR_CELL_OVERFLOW)
+            return fail(WC_ERR_NUMERIC, "a cell row held more than %u particles (a collapsed or non-finite state)",
+                        3u * MAX_CELL_PARTICLES);
         return fail(WC_ERR_TIMEOUT, "a tensor-core GEMM or scan wait exceeded its limit (flags %u)", *s->h_err);
     }
     return WC_OK;
