@@ -39,9 +39,11 @@ constexpr uint32_t WAIT_LIMIT = 1u << 22;
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
 
+// Two buffers of each operand tile: the threads stage slice k+1 into one while the tensor core
+// still reads slice k from the other.
 struct __align__(1024) Tiles {
-    __nv_bfloat16 a[BM * BK];  // 16 KB
-    __nv_bfloat16 b[BN * BK];  // 16 KB
+    __nv_bfloat16 a[2][BM * BK];  // 2 x 16 KB
+    __nv_bfloat16 b[2][BN * BK];  // 2 x 16 KB
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -105,24 +107,60 @@ __device__ __forceinline__ void stage(const OperandSrc& s, __nv_bfloat16* tile, 
             *reinterpret_cast<uint4*>(base + tile_off(r, 8u * g)) = v;
         }
     } else {
-        // 1,024 chunks of 8 consecutive logical rows at one k: src[k * ld + r .. r + 7].
-        for (uint32_t id = threadIdx.x; id < (uint32_t)(BM * BK / 8); id += THREADS) {
-            const uint32_t k = id >> 4, rg = id & 15u;
-            const uint32_t kk = k0 + k, r = row0 + 8u * rg;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (kk < s.ncols && r < s.nrows) v = __ldg(reinterpret_cast<const uint4*>(s.p + (size_t)kk * s.ld + r));
-            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+        // 128 blocks of 8 logical rows x 8 k: eight 16-byte loads (8 rows at one k each),
+        // transposed in registers with byte permutes into eight 16-byte core-matrix rows.
+        for (uint32_t b = threadIdx.x; b < (uint32_t)((BM / 8) * (BK / 8)); b += THREADS) {
+            const uint32_t kg = b >> 4, rg = b & 15u;
+            const uint32_t r = row0 + 8u * rg;
+            uint4 v[8];
 #pragma unroll
-            for (uint32_t j = 0; j < 8; ++j)
-                *reinterpret_cast<__nv_bfloat16*>(base + tile_off(8u * rg + j, k)) = e[j];
+            for (uint32_t e = 0; e < 8; ++e) {
+                const uint32_t kk = k0 + 8u * kg + e;
+                v[e] = make_uint4(0u, 0u, 0u, 0u);
+                if (kk < s.ncols && r < s.nrows) v[e] = __ldg(reinterpret_cast<const uint4*>(s.p + (size_t)kk * s.ld + r));
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j) {
+                // row 8 rg + j: element e of the output row is element j of v[e]
+                const uint32_t sel = (j & 1u) ? 0x7632u : 0x5410u;
+                const uint32_t q = j >> 1;
+                auto word = [&](const uint4& x) { return q == 0 ? x.x : q == 1 ? x.y : q == 2 ? x.z : x.w; };
+                uint4 w;
+                w.x = __byte_perm(word(v[0]), word(v[1]), sel);
+                w.y = __byte_perm(word(v[2]), word(v[3]), sel);
+                w.z = __byte_perm(word(v[4]), word(v[5]), sel);
+                w.w = __byte_perm(word(v[6]), word(v[7]), sel);
+                *reinterpret_cast<uint4*>(base + tile_off(8u * rg + j, 8u * kg)) = w;
+            }
         }
+    }
+}
+
+// x[0..ncols) += r[0..ncols) (bf16): 16-byte loads when the row segment is whole and aligned.
+__device__ __forceinline__ void add_row(float x[32], const __nv_bfloat16* r, uint32_t ncols) {
+    if (ncols == 32u && (reinterpret_cast<uintptr_t>(r) & 15u) == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(r) + q);
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float2 f = __bfloat1622float2(h[k]);
+                x[8 * q + 2 * k] += f.x;
+                x[8 * q + 2 * k + 1] += f.y;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if ((uint32_t)j < ncols) x[j] += __bfloat162float(r[j]);
     }
 }
 
 __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_t* err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     Tiles& t = *reinterpret_cast<Tiles*>(smem_raw);
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[2];  // MMA completion per operand buffer
     __shared__ uint32_t tmem_slot;
     __shared__ int s_failed;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -132,7 +170,8 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
     const uint32_t k_end = min(g.k, k_begin + g.k_chunk);
 
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[1])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_failed = 0;
     }
@@ -150,22 +189,26 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
     // B is staged as B^T (rows = output columns n, columns = k).
     OperandSrc B{g.b, nullptr, nullptr, g.ldb, 0u, 0u, g.n, g.k, g.b_rowmajor};
 
-    const uint32_t a_base = smem_addr(t.a), b_base = smem_addr(t.b);
-    uint32_t phase = 0;
+    uint32_t phase[2] = {0u, 0u};
+    bool pending[2] = {false, false};  // an MMA batch reading this buffer may still run
     bool ok = true;
     uint32_t issued = 0;
+    int last = -1;
     for (uint32_t k0 = k_begin; k0 < k_end; k0 += BK) {
-        if (issued) {
-            // The previous slice's MMAs must finish reading the tiles before they are rewritten.
-            if (!mbar_wait(smem_addr(&mbar), phase)) ok = false;
-            phase ^= 1u;
+        const int buf = (int)(issued & 1u);
+        if (pending[buf]) {
+            // The batch two slices back read this buffer: it must finish before the rewrite.
+            if (!mbar_wait(smem_addr(&mbar[buf]), phase[buf])) ok = false;
+            phase[buf] ^= 1u;
+            pending[buf] = false;
         }
-        stage(A, t.a, m0, k0);
-        stage(B, t.b, n0, k0);
+        stage(A, t.a[buf], m0, k0);
+        stage(B, t.b[buf], n0, k0);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a_base = smem_addr(t.a[buf]), b_base = smem_addr(t.b[buf]);
 #pragma unroll
             for (uint32_t j = 0; j < BK / 16; ++j) {
                 const uint64_t ad = smem_desc(a_base + 256u * j);
@@ -177,13 +220,16 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
                     "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_addr(&mbar))
+                             smem_addr(&mbar[buf]))
                          : "memory");
         }
+        pending[buf] = true;
+        last = buf;
         ++issued;
     }
-    if (issued) {
-        if (!mbar_wait(smem_addr(&mbar), phase)) ok = false;
+    // The last commit covers every MMA issued before it; the other buffer's arrival needs no wait.
+    if (last >= 0) {
+        if (!mbar_wait(smem_addr(&mbar[last]), phase[last])) ok = false;
     }
     if (!ok) atomicOr(&s_failed, 1);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -217,31 +263,34 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
             for (int j = 0; j < 32; ++j)
                 if ((uint32_t)j < ncols) x[j] += __ldg(g.bias + col0 + j);
         }
-        if (g.add1) {
-            const __nv_bfloat16* r1 = g.add1 + (size_t)__ldg(g.add1_idx + row) * g.ld_add + col0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if ((uint32_t)j < ncols) x[j] += __bfloat162float(r1[j]);
-        }
-        if (g.add2) {
-            const __nv_bfloat16* r2 = g.add2 + (size_t)__ldg(g.add2_idx + row) * g.ld_add + col0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if ((uint32_t)j < ncols) x[j] += __bfloat162float(r2[j]);
-        }
+        if (g.add1) add_row(x, g.add1 + (size_t)__ldg(g.add1_idx + row) * g.ld_add + col0, ncols);
+        if (g.add2) add_row(x, g.add2 + (size_t)__ldg(g.add2_idx + row) * g.ld_add + col0, ncols);
         if (g.relu) {
 #pragma unroll
             for (int j = 0; j < 32; ++j) x[j] = fmaxf(x[j], 0.f);
         }
+        // Stores: 16-byte vectors for whole aligned segments, otherwise element by element with
+        // constant indices (the accumulator stays in registers either way).
         if (g.c_f32) {
             float* out = g.c_f32 + (size_t)kz * g.split_stride + (size_t)row * g.ldc + col0;
-            if (g.accumulate) {
-                for (uint32_t j = 0; j < ncols; ++j) out[j] += x[j];
-            } else if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
+            if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
 #pragma unroll
-                for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(out + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+                for (int j = 0; j < 32; j += 4) {
+                    float4* o = reinterpret_cast<float4*>(out + j);
+                    float4 v = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+                    if (g.accumulate) {
+                        const float4 c = *o;
+                        v.x += c.x;
+                        v.y += c.y;
+                        v.z += c.z;
+                        v.w += c.w;
+                    }
+                    *o = v;
+                }
             } else {
-                for (uint32_t j = 0; j < ncols; ++j) out[j] = x[j];
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if ((uint32_t)j < ncols) out[j] = g.accumulate ? out[j] + x[j] : x[j];
             }
         }
         if (g.c_bf16) {
@@ -261,7 +310,9 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
                     *reinterpret_cast<uint4*>(out + j) = w;
                 }
             } else {
-                for (uint32_t j = 0; j < ncols; ++j) out[j] = __float2bfloat16_rn(x[j]);
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if ((uint32_t)j < ncols) out[j] = __float2bfloat16_rn(x[j]);
             }
         }
     }
@@ -275,9 +326,9 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
 
 }  // namespace
 
-// At most four CTAs per SM: 4 x 128 accumulator columns fill the SM's 512 columns of tensor
-// memory exactly, so tcgen05.alloc never has to wait for another CTA.
-size_t gemm_smem_bytes() { return 57u * 1024u; }
+// 64 KB of operand buffers: at most three CTAs per SM, 3 x 128 of the SM's 512 columns of
+// tensor memory, so tcgen05.alloc never has to wait for another CTA.
+size_t gemm_smem_bytes() { return 65u * 1024u; }
 
 wc_status check_gemm(const GemmArgs& g) {
     if (g.m == 0 || g.n == 0) return WC_OK;

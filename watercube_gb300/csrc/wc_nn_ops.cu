@@ -280,15 +280,48 @@ __global__ void segment_sum_kernel(uint32_t nodes, const uint32_t* __restrict__ 
     }
 }
 
-// part[b][c] = sum of rows [b * rpb, (b+1) * rpb) of column c (cols <= 256, one thread each).
-__global__ void colsum_part_kernel(uint32_t rows, uint32_t cols, uint32_t ld, uint32_t rows_per_block,
-                                   const float* __restrict__ x, float* __restrict__ part) {
-    const uint32_t c = threadIdx.x;
-    if (c >= cols) return;
+// part[b][c] = sum of rows [b * rpb, (b+1) * rpb) of column c. Warp w of the block takes rows
+// w, w + 8, ...; lane l columns 4l .. 4l+3 (and 128 further per pass); the 8 warps' sums are
+// added in a fixed order: deterministic.
+constexpr int CS_WARPS = 8;
+constexpr uint32_t CS_ROWS = 256;
+__global__ void __launch_bounds__(CS_WARPS * 32) colsum_part_kernel(uint32_t rows, uint32_t cols, uint32_t ld,
+                                                                   uint32_t rows_per_block, const float* __restrict__ x,
+                                                                   float* __restrict__ part) {
+    __shared__ float s[CS_WARPS][256];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t r0 = blockIdx.x * rows_per_block, r1 = min(rows, r0 + rows_per_block);
-    float a = 0.f;
-    for (uint32_t r = r0; r < r1; ++r) a += x[(size_t)r * ld + c];
-    part[(size_t)blockIdx.x * cols + c] = a;
+    const bool vec = (cols % 4u == 0) && (ld % 4u == 0) && ((reinterpret_cast<uintptr_t>(x) & 15u) == 0);
+    for (uint32_t c0 = 0; c0 < cols; c0 += 128u) {
+        float a[4] = {0.f, 0.f, 0.f, 0.f};
+        const uint32_t c = c0 + 4u * lane;
+        for (uint32_t r = r0 + warp; r < r1; r += CS_WARPS) {
+            const float* src = x + (size_t)r * ld + c;
+            if (vec) {
+                if (c < cols) {
+                    const float4 v = *reinterpret_cast<const float4*>(src);
+                    a[0] += v.x;
+                    a[1] += v.y;
+                    a[2] += v.z;
+                    a[3] += v.w;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (c + k < cols) a[k] += src[k];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (4u * lane + k < 256u) s[warp][4u * lane + k] = a[k];
+        __syncthreads();
+        if (threadIdx.x < 128u && c0 + threadIdx.x < cols) {
+            float t = 0.f;
+            for (int w = 0; w < CS_WARPS; ++w) t += s[w][threadIdx.x];
+            part[(size_t)blockIdx.x * cols + c0 + threadIdx.x] = t;
+        }
+        __syncthreads();
+    }
 }
 
 // out[c] (+)= sum over blocks of part[b][c], fixed order.
@@ -477,12 +510,12 @@ void segment_sum_f32(uint32_t nodes, const uint32_t* rowptr, const uint32_t* idx
         segment_sum_kernel<float><<<blocks_for((size_t)nodes * 32, 256), 256, 0, s>>>(nodes, rowptr, idx, src, out_f32,
                                                                                      out_bf16);
 }
-uint32_t colsum_blocks(uint32_t rows) { return rows ? blocks_for(rows, 1024) : 0; }
+uint32_t colsum_blocks(uint32_t rows) { return rows ? blocks_for(rows, CS_ROWS) : 0; }
 void colsum(uint32_t rows, uint32_t cols, uint32_t ld, const float* x, float* part, float* out, int accumulate,
             cudaStream_t s) {
     const uint32_t blocks = colsum_blocks(rows);
     if (!blocks) return;
-    colsum_part_kernel<<<blocks, 256, 0, s>>>(rows, cols, ld, 1024, x, part);
+    colsum_part_kernel<<<blocks, CS_WARPS * 32, 0, s>>>(rows, cols, ld, CS_ROWS, x, part);
     colsum_final_kernel<<<blocks_for(cols, 128), 128, 0, s>>>(blocks, cols, part, out, accumulate);
 }
 void colsum_partials(uint32_t blocks, uint32_t cols, const float* part, float* out, int accumulate, cudaStream_t s) {
