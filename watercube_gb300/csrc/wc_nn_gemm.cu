@@ -136,6 +136,30 @@ __device__ __forceinline__ void stage(const OperandSrc& s, __nv_bfloat16* tile, 
     }
 }
 
+// The row-major staging as asynchronous copies (cp.async, 16 bytes each, zero-filled outside the
+// matrix): no registers, and the copies of the next slice run while the tensor core works.
+__device__ __forceinline__ void stage_async(const OperandSrc& s, __nv_bfloat16* tile, uint32_t row0, uint32_t k0) {
+    const uint32_t base = smem_addr(tile);
+#pragma unroll 4
+    for (uint32_t id = threadIdx.x; id < (uint32_t)(BM * BK / 8); id += THREADS) {
+        const uint32_t r = id >> 3, g = id & 7u;
+        const uint32_t row = row0 + r, col = k0 + 8u * g;
+        const __nv_bfloat16* src = s.p;  // nothing is read when bytes = 0
+        uint32_t bytes = 0;
+        if (row < s.nrows && col < s.ncols) {
+            const uint32_t src_row = s.rows ? __ldg(s.rows + row) : row;
+            if (s.p2 && col >= s.k_split)
+                src = s.p2 + (size_t)src_row * s.ld2 + (col - s.k_split);
+            else
+                src = s.p + (size_t)src_row * s.ld + col;
+            bytes = 16;
+        }
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(base + tile_off(r, 8u * g)), "l"(src),
+                     "r"(bytes)
+                     : "memory");
+    }
+}
+
 // x[0..ncols) += r[0..ncols) (bf16): 16-byte loads when the row segment is whole and aligned.
 __device__ __forceinline__ void add_row(float x[32], const __nv_bfloat16* r, uint32_t ncols) {
     if (ncols == 32u && (reinterpret_cast<uintptr_t>(r) & 15u) == 0) {
@@ -194,16 +218,44 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
     bool ok = true;
     uint32_t issued = 0;
     int last = -1;
+    // Both operands row-major: asynchronous copies, one slice ahead. Otherwise the threads stage
+    // through registers (the transposed forms), still into the buffer the tensor core is not
+    // reading.
+    const bool async = !A.transposed && !B.transposed;
+    if (async && k_begin < k_end) {
+        stage_async(A, t.a[0], m0, k_begin);
+        stage_async(B, t.b[0], n0, k_begin);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
     for (uint32_t k0 = k_begin; k0 < k_end; k0 += BK) {
         const int buf = (int)(issued & 1u);
-        if (pending[buf]) {
-            // The batch two slices back read this buffer: it must finish before the rewrite.
-            if (!mbar_wait(smem_addr(&mbar[buf]), phase[buf])) ok = false;
-            phase[buf] ^= 1u;
-            pending[buf] = false;
+        if (async) {
+            const uint32_t kn = k0 + BK;
+            if (kn < k_end) {
+                const int nb = buf ^ 1;
+                if (pending[nb]) {
+                    // the batch that read buffer nb (one slice back) must finish before the rewrite
+                    if (!mbar_wait(smem_addr(&mbar[nb]), phase[nb])) ok = false;
+                    phase[nb] ^= 1u;
+                    pending[nb] = false;
+                }
+                stage_async(A, t.a[nb], m0, kn);
+                stage_async(B, t.b[nb], n0, kn);
+                asm volatile("cp.async.commit_group;" ::: "memory");
+                asm volatile("cp.async.wait_group 1;" ::: "memory");  // this slice's copies are done
+            } else {
+                asm volatile("cp.async.wait_group 0;" ::: "memory");
+            }
+        } else {
+            if (pending[buf]) {
+                // The batch two slices back read this buffer: it must finish before the rewrite.
+                if (!mbar_wait(smem_addr(&mbar[buf]), phase[buf])) ok = false;
+                phase[buf] ^= 1u;
+                pending[buf] = false;
+            }
+            stage(A, t.a[buf], m0, k0);
+            stage(B, t.b[buf], n0, k0);
         }
-        stage(A, t.a[buf], m0, k0);
-        stage(B, t.b[buf], n0, k0);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
