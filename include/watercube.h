@@ -520,6 +520,12 @@ WC_API wc_status wc_sort_cells_noalloc(const void* d_positions, uint32_t n, uint
                                        void* d_sorted_positions, void* stream);
 
 /* Make `device` current for handles created afterwards on this thread (one process per GPU). */
+/* Test hook, not for production use: with on != 0 the cell scan's look-back polls a descriptor
+   that nothing publishes, so every scan tile after the first gives up after spin_limit polls and
+   the step reports WC_ERR_TIMEOUT (the tables of that step are invalid, every access stays in
+   bounds); on = 0 restores normal operation. Applies to the current device, for all handles. */
+WC_API wc_status wc_debug_scan_stall(int on, uint32_t spin_limit);
+
 WC_API wc_status wc_set_device(int device);
 WC_API int wc_device_count(void);
 

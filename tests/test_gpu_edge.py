@@ -176,3 +176,26 @@ def test_overfull_rows_refused_by_surface_and_surrogate(gpu):
         with pytest.raises(_abi.WatercubeError) as e:
             sg.sample(f, 1e-3, np.zeros((5, n, 4), np.float32))
         assert e.value.status == _abi.WC_ERR_NUMERIC
+
+
+def test_scan_wait_that_runs_out_is_reported(gpu, wclib):
+    """The look-back's bounded wait made to run out (it polls a descriptor nothing publishes):
+    the step reports WC_ERR_TIMEOUT, the process and the handle stay usable, and with the hook
+    off the next steps equal a fresh run's bit for bit."""
+    p, st = case("dam16k")  # 21^3 cells: three scan tiles
+    _abi.check(wclib.wc_debug_scan_stall(1, 64))
+    try:
+        with fluid(p, st) as f:
+            f.step(1e-3, 2)
+            with pytest.raises(_abi.WatercubeError) as e:
+                f.synchronize()
+            assert e.value.status == _abi.WC_ERR_TIMEOUT
+            _abi.check(wclib.wc_debug_scan_stall(0, 0))
+            f.set_particles(st)
+            f.step(1e-3, 3)
+            again = f.particles()
+    finally:
+        _abi.check(wclib.wc_debug_scan_stall(0, 0))
+    with fluid(p, st) as g:
+        g.step(1e-3, 3)
+        assert g.particles().tobytes() == again.tobytes()

@@ -289,6 +289,7 @@ def _declare(lib) -> None:
                                      C.POINTER(RolloutStats)]),
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_set_device": (S, [C.c_int]),
+        "wc_debug_scan_stall": (S, [S, C.c_uint32]),
         "wc_device_count": (C.c_int, []),
         "wc_alloc_host": (S, [C.c_size_t, C.POINTER(P)]),
         "wc_free_host": (None, [P]),

@@ -33,8 +33,34 @@ struct SceneConsts {
     float g[3];
     float mouse_o[3], mouse_d[3];
     int32_t R;
+    uint32_t R_magic;  // ceil(2^32 / R) for R > 1 (division by R as a multiply-high), 0 for R = 1
     uint32_t eos, flags;
 };
+
+// Reciprocal for division by an invariant R > 1 (Granlund and Montgomery): m = ceil(2^32 / R).
+inline uint32_t r_magic(uint32_t R) { return R > 1u ? (uint32_t)(((1ull << 32) + R - 1u) / R) : 0u; }
+
+// q = n / R and n - q R for n < 2^31: the multiply-high estimate with m = ceil(2^32 / R) is the
+// quotient or one more (its error n (m R - 2^32) / (R 2^32) is below 1), so one signed
+// correction makes it exact.
+__host__ __device__ __forceinline__ uint32_t div_R(uint32_t n, uint32_t R, uint32_t magic, uint32_t* rem) {
+    if (R <= 1u) {
+        *rem = 0u;
+        return n;
+    }
+#ifdef __CUDA_ARCH__
+    uint32_t q = __umulhi(n, magic);
+#else
+    uint32_t q = (uint32_t)(((uint64_t)n * magic) >> 32);
+#endif
+    int32_t r = (int32_t)(n - q * R);
+    if (r < 0) {
+        --q;
+        r += (int32_t)R;
+    }
+    *rem = (uint32_t)r;
+    return q;
+}
 
 // Scene tables of a batch of independent scenes in one set of buffers (device memory). Scene s
 // owns particle slots [poff[s], poff[s+1]) and cell keys [coff[s], coff[s] + R_s^3); one global

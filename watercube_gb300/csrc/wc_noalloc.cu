@@ -117,6 +117,7 @@ WC_API wc_status wc_sort_cells_noalloc(const void* d_positions, uint32_t n, uint
     wc::SceneConsts sc{};
     sc.bin = bin_size;
     sc.R = (int32_t)grid_res;
+    sc.R_magic = wc::r_magic(grid_res);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // The histogram and the error word must start at zero; earlier calls leave them dirty.
     WC_CUDA_TRY(cudaMemsetAsync(d.counts, 0, sizeof(uint32_t) * C, s));

@@ -62,6 +62,7 @@ SceneConsts make_scene_consts(const wc_params& p) {
         c.mouse_d[a] = p.mouse_dir[a];
     }
     c.R = (int32_t)p.grid_res;
+    c.R_magic = r_magic(p.grid_res);
     c.eos = p.eos;
     c.flags = p.flags;
     return c;

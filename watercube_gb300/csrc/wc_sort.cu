@@ -17,11 +17,17 @@
 #include <cuda_runtime.h>
 
 #include "wc_internal.h"
+#include "wc_util.h"
 
 namespace wc {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+
+// Test hook of the look-back (wc_debug_scan_stall): its spin limit, and a switch that makes it
+// poll a descriptor nothing publishes, so that every tile after the first runs its wait out.
+__device__ uint32_t g_scan_spin_limit = SCAN_SPIN_LIMIT;
+__device__ uint32_t g_scan_stall = 0;
 constexpr unsigned long long DESC_AGG = 1ull << 62;      // tile aggregate published
 constexpr unsigned long long DESC_PREFIX = 2ull << 62;   // inclusive prefix published
 constexpr unsigned long long DESC_VALUE = (1ull << 62) - 1;
@@ -183,11 +189,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_cells_kernel(uint32_t* __re
         } else {
             st_volatile_u64(desc + tile, DESC_AGG | tile_total);
             uint32_t j = tile - 1, spins = 0;
+            const uint32_t limit = g_scan_spin_limit;
+            const bool stall = g_scan_stall != 0u;
             for (;;) {
-                const unsigned long long d = ld_volatile_u64(desc + j);
+                const unsigned long long d = stall ? 0ull : ld_volatile_u64(desc + j);
                 const unsigned long long flag = d >> 62;
                 if (flag == 0ull) {
-                    if (++spins > SCAN_SPIN_LIMIT) {  // bounded: report and publish what we have
+                    if (++spins > limit) {  // bounded: report and publish what we have
                         atomicOr(err, DEVERR_SCAN_TIMEOUT);
                         break;
                     }
@@ -338,3 +346,12 @@ void launch_l2_flush(const float4* buf, size_t n4, float* sink, cudaStream_t s) 
 }
 
 }  // namespace wc
+
+extern "C" WC_API wc_status wc_debug_scan_stall(int on, uint32_t spin_limit) {
+    wc::clear_error();
+    const uint32_t stall = on ? 1u : 0u;
+    const uint32_t limit = on ? spin_limit : wc::SCAN_SPIN_LIMIT;
+    WC_CUDA_TRY(cudaMemcpyToSymbol(wc::g_scan_stall, &stall, sizeof stall));
+    WC_CUDA_TRY(cudaMemcpyToSymbol(wc::g_scan_spin_limit, &limit, sizeof limit));
+    return WC_OK;
+}

@@ -103,13 +103,16 @@ struct CellRows {
 
 // Row r = (dy, dz) = (r % 3 - 1, r / 3 - 1) of cell c: cells x-1..x+1 of that row, which are
 // consecutive keys, hence one slot range [start[first], start[last + 1]).
-__device__ __forceinline__ CellRows cell_rows(const uint32_t* __restrict__ start, uint32_t n, int32_t R, uint32_t c,
-                                              uint32_t lane) {
+__device__ __forceinline__ CellRows cell_rows(const uint32_t* __restrict__ start, uint32_t n, int32_t R,
+                                              uint32_t R_magic, uint32_t c, uint32_t lane) {
     CellRows cr;
     cr.cend = min(__ldg(start + c + 1), n);
     cr.cbeg = min(__ldg(start + c), cr.cend);
     const uint32_t uR = (uint32_t)R;
-    const int cx = (int)(c % uR), cy = (int)((c / uR) % uR), cz = (int)(c / (uR * uR));
+    uint32_t rx, ry;
+    const uint32_t q = div_R(c, uR, R_magic, &rx);
+    const uint32_t qz = div_R(q, uR, R_magic, &ry);
+    const int cx = (int)rx, cy = (int)ry, cz = (int)qz;
     uint32_t lo = 0, hi = 0;
     if (lane < 9u) {
         const int yy = cy + (int)(lane % 3u) - 1;
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
             sc = sc0;
         }
         const f2 cull2 = pk(sc.cull, sc.cull);
-        const CellRows cr = cell_rows(start + coff, n, sc.R, cg - coff, lane);
+        const CellRows cr = cell_rows(start + coff, n, sc.R, sc.R_magic, cg - coff, lane);
         if (cr.cend - cr.cbeg > MAX_CELL_PARTICLES) {
             // not evaluated (see MAX_CELL_PARTICLES): NaN density and pressure, reported
             for (uint32_t i = cr.cbeg + lane; i < cr.cend; i += 32u) {
@@ -588,7 +591,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
         } else {
             sc = sc0;
         }
-        const CellRows cr = cell_rows(start + coff, n, sc.R, cg - coff, lane);
+        const CellRows cr = cell_rows(start + coff, n, sc.R, sc.R_magic, cg - coff, lane);
         const uint32_t ncell = cr.cend - cr.cbeg;
         if (ncell > MAX_CELL_PARTICLES) {
             // not evaluated (see MAX_CELL_PARTICLES): the particles keep their state, reported
