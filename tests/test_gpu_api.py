@@ -55,6 +55,31 @@ def test_host_copies_round_trip(gpu):
         assert f.particles(_abi.WC_BUFFER_SORTED).tobytes() == st2.tobytes()
 
 
+def test_pinned_host_copies_round_trip(gpu):
+    """Pinned host buffers (the end-to-end benchmark's) give the same results as pageable ones."""
+    from watercube_gb300.fluid import PinnedBuffer
+
+    p, st = case("dam16k")
+    n = st.shape[0]
+    hin, hout = PinnedBuffer(32 * n), PinnedBuffer(32 * n)
+    try:
+        a_in, a_out = hin.particles(n), hout.particles(n)
+        a_in[:] = st
+        a_in["velocity"] = 0.125
+        with fluid(p, st) as f:
+            f.set_particles(a_in)
+            assert f.particles().tobytes() == a_in.tobytes()
+            f.step(1e-3, 2)
+            lib = _abi.lib()
+            _abi.check(lib.wc_fluid_get_particles(f._handle, _abi.WC_BUFFER_STATE, a_out.ctypes.data, n))
+            assert a_out.tobytes() == f.particles().tobytes()
+            _abi.check(lib.wc_fluid_get_particles(f._handle, _abi.WC_BUFFER_SORTED, a_out.ctypes.data, n))
+            assert a_out.tobytes() == f.particles(_abi.WC_BUFFER_SORTED).tobytes()
+    finally:
+        hin.free()
+        hout.free()
+
+
 def test_set_particles_restarts_tracked_ids(gpu):
     p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
     with fluid(p, st) as f:
