@@ -525,6 +525,10 @@ WC_API wc_status wc_sort_cells_noalloc(const void* d_positions, uint32_t n, uint
    the step reports WC_ERR_TIMEOUT (the tables of that step are invalid, every access stays in
    bounds); on = 0 restores normal operation. Applies to the current device, for all handles. */
 WC_API wc_status wc_debug_scan_stall(int on, uint32_t spin_limit);
+/* Test hook, not for production use: after `after` more successful device allocations, every
+   allocation the library makes fails with WC_ERR_OOM (its callers unwind and free what they
+   hold); after < 0 switches the hook off. Process-wide. */
+WC_API void wc_debug_fail_allocations(long long after);
 
 WC_API wc_status wc_set_device(int device);
 WC_API int wc_device_count(void);

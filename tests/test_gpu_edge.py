@@ -199,3 +199,61 @@ def test_scan_wait_that_runs_out_is_reported(gpu, wclib):
     with fluid(p, st) as g:
         g.step(1e-3, 3)
         assert g.particles().tobytes() == again.tobytes()
+
+
+def test_allocation_failures_unwind_cleanly(gpu, wclib):
+    """Every device allocation of fluid, batch, surface and surrogate creation made to fail in
+    turn: each call reports WC_ERR_OOM, frees what it held, and the next creation succeeds."""
+    torch = pytest.importorskip("torch")
+    from watercube_gb300.batch import Batch, batch_specs, scene_params, scene_particles
+    from watercube_gb300.surface import Surface
+    from watercube_gb300.surrogate import Surrogate
+
+    p, st = case("dam16k")
+    specs = batch_specs(2, 1024, 2048, seed=1)
+    prm = [scene_params(x) for x in specs]
+    init = [scene_particles(x, q) for x, q in zip(specs, prm)]
+
+    def make_fluid():
+        f = Fluid.create("a", p)
+        try:
+            f.setup(st)
+            f.step(1e-3, 1)
+            f.synchronize()
+        finally:
+            f.close()
+
+    def make_batch():
+        with Batch(prm, init) as b:
+            b.step(1e-3, 1)
+
+    def make_surface():
+        with fluid(p, st) as f, Surface(24) as s:
+            s.extract(f)
+
+    def make_surrogate():
+        with Surrogate(layers=1) as s:
+            pass
+
+    for make in (make_fluid, make_batch, make_surface, make_surrogate):
+        make()  # warm: lazily created library state is in place before the baseline
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        failures = 0
+        for k in range(64):
+            wclib.wc_debug_fail_allocations(k)
+            try:
+                make()
+                break
+            except _abi.WatercubeError as e:
+                assert e.status == _abi.WC_ERR_OOM, (make.__name__, k, str(e))
+                failures += 1
+            finally:
+                wclib.wc_debug_fail_allocations(-1)
+        else:
+            pytest.fail(f"{make.__name__} never succeeded")
+        assert failures > 0, make.__name__
+        make()
+        torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info()[0]
+        assert free0 - free1 < 16 << 20, (make.__name__, free0 - free1)  # nothing leaked

@@ -290,6 +290,7 @@ def _declare(lib) -> None:
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_set_device": (S, [C.c_int]),
         "wc_debug_scan_stall": (S, [S, C.c_uint32]),
+        "wc_debug_fail_allocations": (None, [C.c_longlong]),
         "wc_device_count": (C.c_int, []),
         "wc_alloc_host": (S, [C.c_size_t, C.POINTER(P)]),
         "wc_free_host": (None, [P]),

@@ -34,7 +34,7 @@ template <class T>
 wc_status dalloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) return WC_OK;
-    WC_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
+    WC_TRY(::wc::device_alloc(reinterpret_cast<void**>(p), count * sizeof(T)));
     return WC_OK;
 }
 
@@ -549,6 +549,7 @@ WC_API void wc_batch_destroy(wc_batch* b) {
 
 WC_API wc_status wc_batch_set_particles(wc_batch* b, const wc_particle* in, uint64_t total) {
     clear_error();
+    WC_NVTX("wc_batch_set_particles");
     WC_TRY(require(b, false));
     if (total != b->n) return fail(WC_ERR_INVALID_ARG, "%llu particles given, batch holds %llu",
                                    (unsigned long long)total, (unsigned long long)b->n);
@@ -575,6 +576,7 @@ WC_API wc_status wc_batch_setup(wc_batch* b, const wc_particle* initial, uint64_
 
 WC_API wc_status wc_batch_set_recording(wc_batch* b, int on) {
     clear_error();
+    WC_NVTX("wc_batch_setup");
     WC_TRY(require(b, false));
     if (on && !b->d.accel) {
         WC_TRY(dalloc(&b->d.accel, b->n));
@@ -607,6 +609,7 @@ WC_API wc_status wc_batch_get_ids(wc_batch* b, uint32_t* out, uint64_t total) {
 
 WC_API wc_status wc_batch_get_particles(wc_batch* b, wc_particle* out, uint64_t total) {
     clear_error();
+    WC_NVTX("wc_batch_get_particles");
     WC_TRY(require(b, false));
     if (total != b->n) return fail(WC_ERR_INVALID_ARG, "%llu particles asked, batch holds %llu",
                                    (unsigned long long)total, (unsigned long long)b->n);
@@ -620,6 +623,7 @@ WC_API wc_status wc_batch_get_particles(wc_batch* b, wc_particle* out, uint64_t 
 
 WC_API wc_status wc_batch_step(wc_batch* b, float dt, uint32_t nsteps) {
     clear_error();
+    WC_NVTX("wc_batch_step");
     WC_TRY(require(b, true));
     b->in.dt = dt;
     for (uint32_t s = 0; s < nsteps; ++s) WC_TRY(launch(b, b->in));
@@ -650,6 +654,7 @@ WC_API wc_status wc_batch_diagnostics(wc_batch* b, double* out) {
 
 WC_API wc_status wc_batch_time_steps(wc_batch* b, float dt, uint32_t nsteps, int flush_l2, float* step_ms) {
     clear_error();
+    WC_NVTX("wc_batch_time_steps");
     WC_TRY(require(b, true));
     if (!step_ms && nsteps) return fail(WC_ERR_INVALID_ARG, "null step_ms");
     if (flush_l2 && !b->flush_buf) {
@@ -718,6 +723,7 @@ WC_API wc_status wc_batch_set_tuning(wc_batch* b, const wc_tuning* t) {
 
 WC_API wc_status wc_batch_tune(wc_batch* b, float dt, wc_tuning* out) {
     clear_error();
+    WC_NVTX("wc_batch_tune");
     WC_TRY(require(b, true));
     const TuneKey key{b->n, b->cells_cap};
     wc_tuning cached;

@@ -54,7 +54,7 @@ template <class T>
 wc_status dalloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) return WC_OK;
-    WC_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
+    WC_TRY(::wc::device_alloc(reinterpret_cast<void**>(p), count * sizeof(T)));
     return WC_OK;
 }
 
@@ -298,6 +298,7 @@ WC_API void wc_fluid_destroy(wc_fluid* f) {
 
 WC_API wc_status wc_fluid_setup(wc_fluid* f, const wc_particle* initial, uint32_t n) {
     clear_error();
+    WC_NVTX("wc_fluid_setup");
     WC_TRY(require(f, false));
     if (n != f->d.n) return fail(WC_ERR_INVALID_ARG, "setup with %u particles, handle holds %u", n, f->d.n);
     if (n && !initial) return fail(WC_ERR_INVALID_ARG, "null initial particles");
@@ -309,6 +310,7 @@ WC_API wc_status wc_fluid_setup(wc_fluid* f, const wc_particle* initial, uint32_
 
 WC_API wc_status wc_fluid_update(wc_fluid* f, double time) {
     clear_error();
+    WC_NVTX("wc_fluid_update");
     WC_TRY(require(f, true));
     const float dt = (float)time * f->params.time_scale;  // Fluid.cpp:308
     f->in.dt = dt;
@@ -317,6 +319,7 @@ WC_API wc_status wc_fluid_update(wc_fluid* f, double time) {
 
 WC_API wc_status wc_fluid_step(wc_fluid* f, float dt, uint32_t nsteps) {
     clear_error();
+    WC_NVTX("wc_fluid_step");
     WC_TRY(require(f, true));
     f->in.dt = dt;
     for (uint32_t s = 0; s < nsteps; ++s) WC_TRY(launch_step(f, f->in));
@@ -325,6 +328,7 @@ WC_API wc_status wc_fluid_step(wc_fluid* f, float dt, uint32_t nsteps) {
 
 WC_API wc_status wc_fluid_sort(wc_fluid* f) {
     clear_error();
+    WC_NVTX("wc_fluid_sort");
     WC_TRY(require(f, true));
     enqueue_sort(f);
     return check_launch();
@@ -332,6 +336,7 @@ WC_API wc_status wc_fluid_sort(wc_fluid* f) {
 
 WC_API wc_status wc_fluid_density(wc_fluid* f) {
     clear_error();
+    WC_NVTX("wc_fluid_density");
     WC_TRY(require(f, true));
     launch_density(f->d, f->sc, f->ld, f->stream);
     return check_launch();
@@ -339,6 +344,7 @@ WC_API wc_status wc_fluid_density(wc_fluid* f) {
 
 WC_API wc_status wc_fluid_integrate(wc_fluid* f, float dt) {
     clear_error();
+    WC_NVTX("wc_fluid_integrate");
     WC_TRY(require(f, true));
     StepInputs in = f->in;
     in.dt = dt;
@@ -369,6 +375,7 @@ WC_API wc_status wc_fluid_set_gravity(wc_fluid* f, const float gravity[3]) {
 
 WC_API wc_status wc_fluid_get_particles(wc_fluid* f, int buffer, wc_particle* out, uint32_t n) {
     clear_error();
+    WC_NVTX("wc_fluid_get_particles");
     WC_TRY(require(f, false));
     if (buffer != WC_BUFFER_STATE && buffer != WC_BUFFER_SORTED)
         return fail(WC_ERR_INVALID_ARG, "unknown buffer %d", buffer);
@@ -385,6 +392,7 @@ WC_API wc_status wc_fluid_get_particles(wc_fluid* f, int buffer, wc_particle* ou
 
 WC_API wc_status wc_fluid_set_particles(wc_fluid* f, int buffer, const wc_particle* in, uint32_t n) {
     clear_error();
+    WC_NVTX("wc_fluid_set_particles");
     WC_TRY(require(f, false));
     if (buffer != WC_BUFFER_STATE && buffer != WC_BUFFER_SORTED)
         return fail(WC_ERR_INVALID_ARG, "unknown buffer %d", buffer);
@@ -516,6 +524,7 @@ WC_API const char* wc_step_kernel_name(uint32_t index) {
 WC_API wc_status wc_fluid_time_steps(wc_fluid* f, float dt, uint32_t nsteps, int flush_l2, float* step_ms,
                                      float* kernel_ms) {
     clear_error();
+    WC_NVTX("wc_fluid_time_steps");
     WC_TRY(require(f, true));
     if (!step_ms && nsteps) return fail(WC_ERR_INVALID_ARG, "null step_ms");
     if (flush_l2 && !f->flush_buf) {

@@ -1,6 +1,7 @@
 // wc_params.cpp — host-only parts of the C ABI: parameter presets and derivation (the
 // reference's Fluid constructor and Fluid::setup, src/core/Fluid.cpp:9-27 and :203-216),
 // initial-state generators (Fluid::generateInitialParticles, :104-134), error strings.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -36,6 +37,33 @@ wc_status fail(wc_status s, const char* fmt, ...) {
 
 void clear_error() { g_last_error.clear(); }
 const char* last_error() { return g_last_error.c_str(); }
+
+namespace {
+std::atomic<long long> g_allocs_left{-1};  // -1: off; n >= 0: allocations that still succeed
+}
+
+wc_status device_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    if (!bytes) return WC_OK;
+    long long left = g_allocs_left.load();
+    while (left >= 0) {
+        if (left == 0) return fail(WC_ERR_OOM, "device allocation of %zu bytes refused by the test hook", bytes);
+        if (g_allocs_left.compare_exchange_weak(left, left - 1)) break;
+    }
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? WC_ERR_OOM : WC_ERR_CUDA, "cudaMalloc(%zu): %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    return WC_OK;
+}
+
+}  // namespace wc
+
+extern "C" WC_API void wc_debug_fail_allocations(long long after) { wc::g_allocs_left.store(after < 0 ? -1 : after); }
+
+namespace wc {
 
 SceneConsts make_scene_consts(const wc_params& p) {
     SceneConsts c;

@@ -95,6 +95,7 @@ extern "C" {
 
 WC_API wc_status wc_fluid_save_snapshot(wc_fluid* f, const char* path, uint64_t seed) {
     clear_error();
+    WC_NVTX("wc_fluid_save_snapshot");
     if (!f || !path) return fail(WC_ERR_INVALID_ARG, "null argument");
     WC_TRY(wc_fluid_synchronize(f));
     FluidInternals fi = fluid_internals(f);
@@ -149,6 +150,7 @@ WC_API wc_status wc_snapshot_read_header(const char* path, wc_snapshot_header* o
 
 WC_API wc_status wc_fluid_load_snapshot(wc_fluid* f, const char* path) {
     clear_error();
+    WC_NVTX("wc_fluid_load_snapshot");
     if (!f) return fail(WC_ERR_INVALID_ARG, "null fluid");
     wc_snapshot_header hdr;
     std::vector<float4> p, v;

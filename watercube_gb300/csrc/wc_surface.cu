@@ -274,7 +274,7 @@ template <class T>
 wc_status dalloc(T** p, size_t count) {
     *p = nullptr;
     if (!count) return WC_OK;
-    WC_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
+    WC_TRY(::wc::device_alloc(reinterpret_cast<void**>(p), count * sizeof(T)));
     return WC_OK;
 }
 
@@ -376,6 +376,7 @@ WC_API void wc_surface_destroy(wc_surface* s) {
 
 WC_API wc_status wc_surface_extract(wc_surface* s, wc_fluid* f, uint64_t* num_triangles) {
     clear_error();
+    WC_NVTX("wc_surface_extract");
     if (!s || !f) return fail(WC_ERR_INVALID_ARG, "null argument");
     FluidInternals fi = fluid_internals(f);
     const DevBuffers& d = *fi.d;

@@ -57,7 +57,7 @@ template <class T>
 wc_status dalloc(T** p, size_t count) {
     *p = nullptr;
     if (!count) return WC_OK;
-    WC_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
+    WC_TRY(::wc::device_alloc(reinterpret_cast<void**>(p), count * sizeof(T)));
     return WC_OK;
 }
 template <class T>
@@ -916,6 +916,7 @@ WC_API wc_status wc_surrogate_zero_grads(wc_surrogate* s) {
 WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, const float* host_hist,
                                      const float* host_target) {
     clear_error();
+    WC_NVTX("wc_surrogate_sample");
     if (!s || !f || !host_hist) return fail(WC_ERR_INVALID_ARG, "null argument");
     if (!(dt > 0.f)) return fail(WC_ERR_INVALID_ARG, "dt must be > 0");
     s->dt = dt;
@@ -938,6 +939,7 @@ WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, con
 
 WC_API wc_status wc_surrogate_forward_backward(wc_surrogate* s, int do_backward, double* loss) {
     clear_error();
+    WC_NVTX("wc_surrogate_forward_backward");
     if (!s || !s->fluid) return fail(WC_ERR_STATE, "no sample loaded (wc_surrogate_sample)");
     if (do_backward && !s->has_target) return fail(WC_ERR_STATE, "backward needs a sample with targets");
     WC_TRY(forward(s));
@@ -978,6 +980,7 @@ WC_API wc_status wc_surrogate_predictions(wc_surrogate* s, float* host_out, uint
 
 WC_API wc_status wc_surrogate_adam(wc_surrogate* s, float lr, float grad_scale) {
     clear_error();
+    WC_NVTX("wc_surrogate_adam");
     if (!s) return fail(WC_ERR_INVALID_ARG, "null surrogate");
     ++s->adam_step;
     adam(s->nparams, s->w, s->g, s->m, s->v, lr, 0.9f, 0.999f, 1e-8f, s->adam_step, grad_scale, s->stream);
@@ -989,6 +992,7 @@ WC_API wc_status wc_surrogate_adam(wc_surrogate* s, float lr, float grad_scale) 
 WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t K,
                                       float tolerance, int mode, const float* hist, wc_rollout_stats* out) {
     clear_error();
+    WC_NVTX("wc_surrogate_rollout");
     if (!out) return fail(WC_ERR_INVALID_ARG, "null argument");
     std::memset(out, 0, sizeof *out);
     if (!f || (mode != WC_ROLLOUT_SPH && !s)) return fail(WC_ERR_INVALID_ARG, "null argument");
