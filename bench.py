@@ -100,7 +100,7 @@ class Clocks:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -514,7 +514,9 @@ def run_batch(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 1000 for the single scenes, 200 for batch512, 16 for rollout1m; "
+                         "20 for --impl reference)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512", "rollout1m"], default="dam1m")
@@ -524,6 +526,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        if args.impl == "reference":
+            args.steps = 20
+        else:
+            args.steps = {"batch512": 200, "rollout1m": 16}.get(args.workload, 1000)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch512":
