@@ -260,10 +260,17 @@ def run_reference(args):
 
 
 def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01) -> dict:
-    """Plain SPH, surrogate and stale-acceleration rollouts of `steps` steps from `st`, each on a
-    fresh fluid; the surrogate uses the committed trained weights when present."""
+    """Plain SPH, surrogate, stale-acceleration and hybrid rollouts of `steps` steps from `st`, each
+    on a fresh fluid; the network uses the committed trained weights when present."""
     from watercube_gb300.fluid import Fluid
-    from watercube_gb300.surrogate import WC_ROLLOUT_SPH, WC_ROLLOUT_STALE, WC_ROLLOUT_SURROGATE, Surrogate, rollout
+    from watercube_gb300.surrogate import (
+        WC_ROLLOUT_HYBRID,
+        WC_ROLLOUT_SPH,
+        WC_ROLLOUT_STALE,
+        WC_ROLLOUT_SURROGATE,
+        Surrogate,
+        rollout,
+    )
     from watercube_gb300.train_surrogate import DEFAULT_WEIGHTS, load_weights
 
     trained = DEFAULT_WEIGHTS.is_file()
@@ -272,15 +279,13 @@ def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01) -> 
            "weights": DEFAULT_WEIGHTS.relative_to(REPO).as_posix() if trained else "untrained (seed 1)"}
     keep = ("particle_steps_per_s", "ms_device", "sph_steps", "surrogate_steps", "judged", "reverted",
             "mean_density_error", "max_density_error")
-    for mode, name in ((WC_ROLLOUT_SPH, "plain"), (WC_ROLLOUT_SURROGATE, "surrogate"), (WC_ROLLOUT_STALE, "stale")):
+    for mode, name in ((WC_ROLLOUT_SPH, "plain"), (WC_ROLLOUT_SURROGATE, "surrogate"), (WC_ROLLOUT_STALE, "stale"),
+                       (WC_ROLLOUT_HYBRID, "hybrid")):
         f = Fluid.create("rollout", p)
         f.setup(st)
-        if mode == WC_ROLLOUT_SURROGATE:
-            rollout(f, dt, 1, K, tolerance, mode, s)  # workspace allocation outside the timed rollout
-            f.setup(st)
-        else:
-            rollout(f, dt, 2, K, tolerance, mode, s)  # graph capture
-            f.setup(st)
+        # graph capture and workspace allocation outside the timed rollout
+        rollout(f, dt, 1 if mode == WC_ROLLOUT_SURROGATE else 2, K, tolerance, mode, s)
+        f.setup(st)
         r = rollout(f, dt, steps, K, tolerance, mode, s)
         d0, d1 = np.array(r["diag_start"]), np.array(r["diag_end"])
         e = {k: r[k] for k in keep}
@@ -291,6 +296,7 @@ def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01) -> 
     s.close()
     out["surrogate_vs_plain"] = out["surrogate"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
     out["stale_vs_plain"] = out["stale"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
+    out["hybrid_vs_plain"] = out["hybrid"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
     return out
 
 

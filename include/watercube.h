@@ -452,9 +452,14 @@ WC_API wc_status wc_surrogate_get_grads(wc_surrogate* s, float* host, uint64_t n
 WC_API wc_status wc_surrogate_zero_grads(wc_surrogate* s);
 /* Load one training sample: the fluid's current particles (positions and velocities, set
    with wc_fluid_set_particles), the velocity history hist[5][n][4] (hist[0] = current
-   velocity, hist[k] = k steps ago, dt apart) and, optionally, the target accelerations
-   target[n][4]. Sorts the fluid and builds the graph and features. */
-WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, const float* hist, const float* target);
+   velocity, hist[k] = k steps ago, dt apart), optionally the target accelerations
+   target[n][4], and optionally the last SPH acceleration stale[n][4] computed stale_age >= 1
+   steps ago (NULL or 0: none; the network then sees zeros there). A sample with a stale
+   acceleration is residual: the network's output stands for the change since then (its loss
+   target is target - stale) and wc_surrogate_predictions returns stale + output. Sorts the
+   fluid and builds the graph and features. */
+WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, const float* hist, const float* target,
+                                     const float* stale, uint32_t stale_age);
 /* Forward pass on the loaded sample; with do_backward, the gradients of the mean squared error
    (per component, outputs scaled by 1 / accel_scale) are added to the accumulated ones. *loss
    (may be NULL) receives that error. */
@@ -483,9 +488,12 @@ typedef struct wc_rollout_stats {
 #define WC_ROLLOUT_SPH 0
 #define WC_ROLLOUT_SURROGATE 1
 #define WC_ROLLOUT_STALE 2
+/* HYBRID: as STALE, but the skipped steps take the last SPH acceleration plus the network's
+   residual, computed with that acceleration and its age as inputs. */
+#define WC_ROLLOUT_HYBRID 3
 
-/* Advance the fluid nsteps in `mode`. In the SURROGATE and STALE modes every K-th step is
-   judged: SPH and the candidate both advance the same state, the SPH densities of the two next
+/* Advance the fluid nsteps in `mode`. In the SURROGATE, STALE and HYBRID modes every K-th step
+   is judged: SPH and the candidate both advance the same state, the SPH densities of the two next
    states are compared particle by particle, and the SPH state is kept (the step is reverted)
    when the mean |rho_candidate / rho_SPH - 1| exceeds `tolerance`. s may be NULL for SPH.
    hist (host, [5][n][4] in state order, as for wc_surrogate_sample) seeds the surrogate's

@@ -19,7 +19,9 @@ Graph: ordered pairs (i, j), i != j, with d2 <= cull, d2 = fma(dz, dz, fma(dy, d
 FP32 (cull = largest float whose square root is below h), edge features from receiver i to
 sender j. Features: node = current velocity / velocity_scale, the four successive velocity
 differences / (dt accel_scale) (FP32), 6 wall distances / h clipped to [0, 1], stiffness /
-rest density * 200, zeros to 32; edge = (x_i - x_j) / h, |x_i - x_j| / h,
+rest density * 200, the last SPH acceleration / accel_scale and its age in steps / 8 (zeros when
+none is given), zeros to 32. With a stale acceleration the sample is residual: the loss target
+is target - stale and the acceleration is stale + output (the caller subtracts and adds it); edge = (x_i - x_j) / h, |x_i - x_j| / h,
 zeros to 16.
 
 Emulated BF16 rounding: the CUDA path keeps features, weights and the stored activations in
@@ -109,7 +111,8 @@ def radius_graph(pos: np.ndarray, cull: float) -> tuple[np.ndarray, np.ndarray]:
     return recv.astype(np.int64), send.astype(np.int64)
 
 
-def node_features(pos, hist, size, h, k_feature, velocity_scale, dt, accel_scale) -> np.ndarray:
+def node_features(pos, hist, size, h, k_feature, velocity_scale, dt, accel_scale, stale=None,
+                  stale_age: int = 0) -> np.ndarray:
     pos = np.asarray(pos, np.float32)
     n = pos.shape[0]
     f = np.zeros((n, NODE_IN), np.float32)
@@ -125,6 +128,10 @@ def node_features(pos, hist, size, h, k_feature, velocity_scale, dt, accel_scale
     for a, w in enumerate(walls):
         f[:, 15 + a] = np.clip(w.astype(np.float32) * inv_h, 0.0, 1.0)
     f[:, 21] = np.float32(k_feature)
+    if stale is not None and stale_age > 0:
+        inv_a = np.float32(1.0) / np.float32(accel_scale)
+        f[:, 22:25] = np.asarray(stale, np.float32)[:, :3] * inv_a
+        f[:, 25] = np.float32(stale_age) * np.float32(0.125)
     return f
 
 
@@ -218,13 +225,15 @@ def cull_threshold(h: float) -> np.float32:
     return x
 
 
-def sample_inputs(state: np.ndarray, hist: np.ndarray, params, velocity_scale: float, dt: float, accel_scale: float):
-    """Graph and features of one sample (state: PARTICLE_DTYPE, hist: (5, n, 4)), as the CUDA path
-    builds them from the same particles."""
+def sample_inputs(state: np.ndarray, hist: np.ndarray, params, velocity_scale: float, dt: float, accel_scale: float,
+                  stale=None, stale_age: int = 0):
+    """Graph and features of one sample (state: PARTICLE_DTYPE, hist: (5, n, 4), stale: (n, 4) or
+    None), as the CUDA path builds them from the same particles."""
     pos = np.asarray(state["position"], np.float32)
     cull = cull_threshold(params.kernel_radius)
     recv, send = radius_graph(pos, cull)
     k_feature = np.float32(params.stiffness) / np.float32(params.rest_density) * np.float32(200.0)
-    xn = node_features(pos, hist, params.size, params.kernel_radius, k_feature, velocity_scale, dt, accel_scale)
+    xn = node_features(pos, hist, params.size, params.kernel_radius, k_feature, velocity_scale, dt, accel_scale,
+                       stale, stale_age)
     xe = edge_features(pos, recv, send, params.kernel_radius)
     return xn, xe, recv, send

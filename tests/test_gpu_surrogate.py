@@ -18,6 +18,7 @@ from watercube_gb300 import _abi
 from watercube_gb300.batch import batch_specs
 from watercube_gb300.fluid import Fluid, dam_break_params, finalize, generate_dam_break
 from watercube_gb300.surrogate import (
+    WC_ROLLOUT_HYBRID,
     WC_ROLLOUT_SPH,
     WC_ROLLOUT_STALE,
     WC_ROLLOUT_SURROGATE,
@@ -80,20 +81,32 @@ def test_param_layout_matches_oracle(gpu, layers):
         assert np.array_equal(s.params(), w2)
 
 
-@pytest.mark.parametrize("layers,n", [(1, 1500), (3, 3000)])
-def test_gradients_match_fp64_oracle(gpu, layers, n):
+@pytest.mark.parametrize("layers,n,age", [(1, 1500, 0), (3, 3000, 0), (2, 2000, 3)])
+def test_gradients_match_fp64_oracle(gpu, layers, n, age):
+    """age > 0 also feeds the last SPH acceleration (age steps old) as the hybrid rollout does."""
     p, state, hist, target = scene(n, seed=layers)
+    stale = None
+    if age:
+        stale = target + np.random.default_rng(age).normal(0.0, 1.0, target.shape).astype(np.float32)
+        stale[:, 3] = 0.0
     with Surrogate(layers=layers, seed=7) as s, Fluid("grad", p) as f:
         w = perturbed_params(s, seed=11)
         s.set_params(w)
         f.setup(state)
-        s.sample(f, 1e-3, hist, target)
+        s.sample(f, 1e-3, hist, target, stale, age)
         s.zero_grads()
         loss = s.forward_backward(True)
         g = s.grads().astype(np.float64)
         pred = s.predictions()
-        xn, xe, recv, send = R.sample_inputs(state, hist, p, s.config.velocity_scale, 1e-3, s.config.accel_scale)
-        ref_loss, ref_g, ref_pred = R.Net(w, layers).loss_and_grads(xn, xe, recv, send, target, s.config.accel_scale)
+        xn, xe, recv, send = R.sample_inputs(state, hist, p, s.config.velocity_scale, 1e-3, s.config.accel_scale,
+                                             stale, age)
+        base = np.zeros_like(target)
+        if age:
+            assert np.all(xn[:, 25] == np.float32(age / 8)) and np.abs(xn[:, 22:25]).max() > 0.1
+            base = stale.astype(np.float64)  # residual sample: target - stale is learnt, stale added back
+        ref_loss, ref_g, ref_pred = R.Net(w, layers).loss_and_grads(xn, xe, recv, send, target - base,
+                                                                    s.config.accel_scale)
+        ref_pred = ref_pred + base[:, :3]
     assert abs(loss - ref_loss) <= 1e-2 * ref_loss
     perr = np.linalg.norm(pred[:, :3] - ref_pred) / np.linalg.norm(ref_pred)
     assert perr <= 2e-2, perr
@@ -213,7 +226,48 @@ def test_rollout_surrogate_steps_follow_network_predictions(gpu):
     np.testing.assert_allclose(got_x, cur["position"], rtol=0, atol=2e-7)
 
 
-@pytest.mark.parametrize("mode", [WC_ROLLOUT_SURROGATE, WC_ROLLOUT_STALE])
+def test_rollout_hybrid_step_follows_network_with_stale_input(gpu):
+    """HYBRID with K = 2 over two steps: a plain SPH step that records the acceleration, then a
+    step integrating the network's prediction made with that acceleration (age 1) and the
+    history shifted by the first step. Made by hand through sample(stale=..., stale_age=1) and
+    the host integrator, the result must agree: the rollout's stale input, its age and its
+    ordering match the training path."""
+    dt = 1e-3
+    p, state, hist, _ = scene(3000, seed=9)
+    n = state.shape[0]
+    p.flags |= _abi.WC_FLAG_TRACK_IDS
+    lib = _abi.lib()
+    with Surrogate(layers=2, seed=4) as s, Fluid("hand", p) as a, Fluid("roll", p) as b:
+        s.set_params(perturbed_params(s, seed=6))
+        a.setup(state)
+        b.setup(state)
+        _abi.check(lib.wc_fluid_set_recording(a._require(), 1))
+        a.step(dt, 1)
+        s1, ids = a.particles(), a.particle_ids()
+        acc = np.zeros((n, 4), np.float32)
+        _abi.check(lib.wc_fluid_get_accelerations(a._require(), _abi._ptr(acc), n))
+        s1_id = np.empty_like(s1)
+        s1_id[ids] = s1
+        acc_id = np.zeros_like(acc)
+        acc_id[ids] = acc
+        h1 = np.concatenate([np.pad(s1_id["velocity"], ((0, 0), (0, 1)))[None], hist[:-1]], axis=0)
+        a.set_particles(s1_id)
+        s.sample(a, dt, h1, stale=acc_id, stale_age=1)
+        s.forward_backward(False)
+        x, v = integrate_host(p, s1_id, s.predictions(), dt)
+        st = s.rollout(b, dt, 2, K=2, tolerance=1e9, mode=WC_ROLLOUT_HYBRID, hist=hist)
+        assert st["sph_steps"] == 1 and st["surrogate_steps"] == 1 and st["judged"] == 0
+        out, bids = b.particles(), b.particle_ids()
+    got_x = np.empty_like(x)
+    got_v = np.empty_like(v)
+    got_x[bids] = out["position"]
+    got_v[bids] = out["velocity"]
+    # tolerances as for the surrogate steps above
+    np.testing.assert_allclose(got_v, v, rtol=0, atol=3e-5)
+    np.testing.assert_allclose(got_x, x, rtol=0, atol=2e-7)
+
+
+@pytest.mark.parametrize("mode", [WC_ROLLOUT_SURROGATE, WC_ROLLOUT_STALE, WC_ROLLOUT_HYBRID])
 @pytest.mark.parametrize("track_ids", [False, True])
 def test_rollout_reverting_every_step_is_plain_sph(gpu, mode, track_ids):
     """K = 1 and tolerance 0 judge and revert every step: the state (and the particle ids) must
@@ -233,7 +287,7 @@ def test_rollout_reverting_every_step_is_plain_sph(gpu, mode, track_ids):
             assert np.array_equal(a.particle_ids(), b.particle_ids())
 
 
-@pytest.mark.parametrize("mode", [WC_ROLLOUT_SURROGATE, WC_ROLLOUT_STALE])
+@pytest.mark.parametrize("mode", [WC_ROLLOUT_SURROGATE, WC_ROLLOUT_STALE, WC_ROLLOUT_HYBRID])
 @pytest.mark.parametrize("tolerance", [0.0, 1e9])
 def test_rollout_bookkeeping(gpu, mode, tolerance):
     p = finalize(dam_break_params(4096))
@@ -244,7 +298,7 @@ def test_rollout_bookkeeping(gpu, mode, tolerance):
         st = s.rollout(f, 1e-3, nsteps, K=K, tolerance=tolerance, mode=mode)
         out = f.particles()
     assert st["steps"] == nsteps
-    first = 1 if mode == WC_ROLLOUT_STALE else 0  # the stale mode's first step is plain SPH
+    first = 0 if mode == WC_ROLLOUT_SURROGATE else 1  # the stale and hybrid modes start with plain SPH
     judged = sum(1 for t in range(first, nsteps) if t % K == 0)
     assert st["judged"] == judged
     assert st["sph_steps"] == judged + first

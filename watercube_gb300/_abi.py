@@ -281,7 +281,7 @@ def _declare(lib) -> None:
         "wc_surrogate_set_params": (S, [P, P, C.c_uint64]),
         "wc_surrogate_get_grads": (S, [P, P, C.c_uint64]),
         "wc_surrogate_zero_grads": (S, [P]),
-        "wc_surrogate_sample": (S, [P, P, C.c_float, P, P]),
+        "wc_surrogate_sample": (S, [P, P, C.c_float, P, P, P, C.c_uint32]),
         "wc_surrogate_forward_backward": (S, [P, S, C.POINTER(C.c_double)]),
         "wc_surrogate_predictions": (S, [P, P, C.c_uint32]),
         "wc_surrogate_adam": (S, [P, C.c_float, C.c_float]),

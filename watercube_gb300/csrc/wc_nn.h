@@ -55,7 +55,8 @@ void graph_fill(const float4* pos, uint32_t n, const uint32_t* start, float bin,
                 const uint32_t* rowptr, uint32_t* col, cudaStream_t s);
 void graph_rev(uint32_t n, const uint32_t* rowptr, const uint32_t* col, uint32_t* recv, uint32_t* rev, cudaStream_t s);
 void node_features(uint32_t n, const float4* pos, const float4* hist, float inv_v, float inv_dv, float inv_h,
-                   float size, float k_feature, __nv_bfloat16* out, cudaStream_t s);
+                   float size, float k_feature, const float4* stale, float inv_a, float age_feature,
+                   __nv_bfloat16* out, cudaStream_t s);
 void edge_features(uint32_t e, const float4* pos, const uint32_t* recv, const uint32_t* col, float inv_h,
                    __nv_bfloat16* out, cudaStream_t s);
 void layernorm(uint32_t rows, const float* y, const float* gamma, const float* beta, const __nv_bfloat16* resid,
@@ -82,6 +83,9 @@ void adam(size_t count, float* w, const float* g, float* m, float* v, float lr, 
 void cast_weight(const float* w, uint32_t k_in, uint32_t n_out, uint32_t k_pad, uint32_t n_pad, __nv_bfloat16* wt,
                  __nv_bfloat16* wk, cudaStream_t s);
 void gather4(uint32_t n, const uint32_t* perm, const float4* src, float4* dst, cudaStream_t s);
+void sub_xyz(uint32_t n, float4* dst, const float4* sub, cudaStream_t s);
+void add_scaled(uint32_t n, const float* pred, uint32_t ldp, float scale, const float4* base, float4* dst,
+                cudaStream_t s);
 void scatter_density(uint32_t n, const uint32_t* ids, const float4* src, float* dst, cudaStream_t s);
 uint32_t rel_err_blocks(uint32_t n);
 void rel_err(uint32_t n, const float* a, const float* b, double* part, cudaStream_t s);

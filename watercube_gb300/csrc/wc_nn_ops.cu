@@ -99,10 +99,12 @@ __global__ void graph_rev_kernel(uint32_t n, const uint32_t* __restrict__ rowptr
 // Node features (32, bf16): the last 5 velocities as the current velocity / v_scale (3) and the
 // four successive differences (v[s-1] - v[s]) * inv_dv (12; inv_dv = 1 / (dt a_scale), so each is
 // a past acceleration on the output scale), wall distances / h clipped to 1 (6), stiffness /
-// rest density * 200 (1), zeros (10). hist[s * n + i] is the velocity s steps ago. The
-// differences are taken in FP32 before the BF16 cast, which would otherwise lose them.
+// rest density * 200 (1), the last SPH acceleration / a_scale (3) and its age in steps / 8 (1)
+// when one is given (zeros otherwise), zeros (6). hist[s * n + i] is the velocity s steps ago.
+// The differences are taken in FP32 before the BF16 cast, which would otherwise lose them.
 __global__ void node_features_kernel(uint32_t n, const float4* __restrict__ pos, const float4* __restrict__ hist,
                                      float inv_v, float inv_dv, float inv_h, float size, float k_feature,
+                                     const float4* __restrict__ stale, float inv_a, float age_feature,
                                      __nv_bfloat16* __restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -126,6 +128,13 @@ __global__ void node_features_kernel(uint32_t n, const float4* __restrict__ pos,
     f[21] = k_feature;
 #pragma unroll
     for (int a = 22; a < 32; ++a) f[a] = 0.f;
+    if (stale) {
+        const float4 sa = stale[i];
+        f[22] = sa.x * inv_a;
+        f[23] = sa.y * inv_a;
+        f[24] = sa.z * inv_a;
+        f[25] = age_feature;
+    }
     __nv_bfloat16* o = out + (size_t)i * 32;
 #pragma unroll
     for (int a = 0; a < 32; ++a) o[a] = __float2bfloat16_rn(f[a]);
@@ -425,6 +434,28 @@ __global__ void integrate_kernel(uint32_t n, const SceneConsts sc, float dt, con
 }
 
 // out[perm[k]] style gather of float4 rows: dst[k] = src[perm[k]] (history follows the sort).
+// dst.xyz -= sub.xyz (the target of a residual sample: the change since the stale acceleration)
+__global__ void sub_xyz_kernel(uint32_t n, float4* __restrict__ dst, const float4* __restrict__ sub) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = dst[i];
+    const float4 b = sub[i];
+    a.x -= b.x;
+    a.y -= b.y;
+    a.z -= b.z;
+    dst[i] = a;
+}
+
+// dst = base + scale * pred[:, 0:3] (a residual prediction added to the stale acceleration)
+__global__ void add_scaled_kernel(uint32_t n, const float* __restrict__ pred, uint32_t ldp, float scale,
+                                  const float4* __restrict__ base, float4* __restrict__ dst) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = pred + (size_t)i * ldp;
+    const float4 b = base[i];
+    dst[i] = make_float4(__fmaf_rn(p[0], scale, b.x), __fmaf_rn(p[1], scale, b.y), __fmaf_rn(p[2], scale, b.z), 0.f);
+}
+
 __global__ void gather4_kernel(uint32_t n, const uint32_t* __restrict__ perm, const float4* __restrict__ src,
                                float4* __restrict__ dst) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -468,10 +499,11 @@ void graph_rev(uint32_t n, const uint32_t* rowptr, const uint32_t* col, uint32_t
     if (n) graph_rev_kernel<<<blocks_for(n, 128), 128, 0, s>>>(n, rowptr, col, recv, rev);
 }
 void node_features(uint32_t n, const float4* pos, const float4* hist, float inv_v, float inv_dv, float inv_h,
-                   float size, float k_feature, __nv_bfloat16* out, cudaStream_t s) {
+                   float size, float k_feature, const float4* stale, float inv_a, float age_feature,
+                   __nv_bfloat16* out, cudaStream_t s) {
     if (n)
         node_features_kernel<<<blocks_for(n, 128), 128, 0, s>>>(n, pos, hist, inv_v, inv_dv, inv_h, size, k_feature,
-                                                                out);
+                                                                stale, inv_a, age_feature, out);
 }
 void edge_features(uint32_t e, const float4* pos, const uint32_t* recv, const uint32_t* col, float inv_h,
                    __nv_bfloat16* out, cudaStream_t s) {
@@ -542,6 +574,13 @@ void integrate(uint32_t n, const SceneConsts& sc, float dt, const float* pred, u
     if (n)
         integrate_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, sc, dt, pred, ldp, a_scale, d.pos_b, d.vel_b, d.ids_b,
                                                             d.pos_a, d.vel_a, d.ids_a);
+}
+void sub_xyz(uint32_t n, float4* dst, const float4* sub, cudaStream_t s) {
+    if (n) sub_xyz_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, dst, sub);
+}
+void add_scaled(uint32_t n, const float* pred, uint32_t ldp, float scale, const float4* base, float4* dst,
+                cudaStream_t s) {
+    if (n) add_scaled_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, pred, ldp, scale, base, dst);
 }
 void gather4(uint32_t n, const uint32_t* perm, const float4* src, float4* dst, cudaStream_t s) {
     if (n) gather4_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, perm, src, dst);

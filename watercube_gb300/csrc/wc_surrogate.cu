@@ -83,7 +83,7 @@ struct Work {
     uint32_t *scan_scratch = nullptr, *scan_words = nullptr;
     unsigned long long* scan_desc = nullptr;
     // inputs (sorted order)
-    float4 *hist_s = nullptr, *target_s = nullptr;
+    float4 *hist_s = nullptr, *target_s = nullptr, *stale_s = nullptr;
     __nv_bfloat16 *xn = nullptr, *xe = nullptr;
     // node side
     __nv_bfloat16 *h = nullptr, *zn0 = nullptr, *P = nullptr, *Q = nullptr, *agg = nullptr, *zn = nullptr, *zd = nullptr;
@@ -101,7 +101,7 @@ struct Work {
 };
 
 void free_work(Work& w) {
-    void* ptrs[] = {w.rowptr, w.col,  w.recv, w.rev,  w.count, w.scan_scratch, w.scan_words, w.scan_desc, w.hist_s,
+    void* ptrs[] = {w.stale_s, w.rowptr, w.col,  w.recv, w.rev,  w.count, w.scan_scratch, w.scan_words, w.scan_desc, w.hist_s,
                     w.target_s, w.xn, w.xe,   w.h,    w.zn0,   w.P,            w.Q,          w.agg,       w.zn,
                     w.zd,     w.yn0,  w.yn,   w.out,  w.stn0,  w.stn,          w.e,          w.ze0,       w.ze,
                     w.ye0,    w.ye,   w.ste0, w.ste,  w.dh,    w.dagg,         w.dtmp_n,     w.dP,        w.dQ,
@@ -133,9 +133,11 @@ struct wc_surrogate {
     wc_fluid* fluid = nullptr;
     uint32_t n = 0, e = 0;
     bool has_target = false;
+    bool has_stale = false;  // the loaded sample is residual: its outputs are added to work.stale_s
     float dt = 1e-3f;  // time step of the loaded sample (velocity differences / dt are features)
     float4* hist_in = nullptr;  // [5 n] in state order (sample / rollout history)
     float4* target_in = nullptr;
+    float4* stale_in = nullptr;  // [n] last SPH acceleration of a sample, state order
     uint32_t cap_in = 0;
     // rollout scratch
     float4 *save_pos = nullptr, *save_vel = nullptr, *alt_pos = nullptr, *alt_vel = nullptr;
@@ -337,6 +339,7 @@ wc_status ensure_work(wc_surrogate* s, uint32_t n, uint32_t e, bool saved) {
     WC_TRY(dalloc(&w.rev, ce));
     WC_TRY(dalloc(&w.hist_s, 5 * (size_t)cn));
     WC_TRY(dalloc(&w.target_s, cn));
+    WC_TRY(dalloc(&w.stale_s, cn));
     WC_TRY(dalloc(&w.xn, (size_t)cn * NODE_IN));
     WC_TRY(dalloc(&w.xe, (size_t)ce * EDGE_IN));
     WC_TRY(dalloc(&w.h, Ln * cn * W));
@@ -430,8 +433,14 @@ wc_status build_graph(wc_surrogate* s, const FluidInternals& fi, uint32_t* e_out
     return WC_OK;
 }
 
-// Features of the sorted sample: hist_s/target_s are gathered by the sort's permutation.
-wc_status prepare_sample(wc_surrogate* s, wc_fluid* f, bool saved) {
+// Features of the sorted sample: hist_s/target_s are gathered by the sort's permutation. `stale`
+// (the last SPH acceleration, `age` steps old; null for none) is in the state order, or already
+// in the sorted order when stale_sorted. A sample with a stale acceleration is residual: the
+// network's output is the change since then (the loss target is target - stale), and the
+// acceleration it stands for is stale + output (added in FP32, so the large part of the
+// acceleration never passes through the BF16 network).
+wc_status prepare_sample(wc_surrogate* s, wc_fluid* f, bool saved, const float4* stale = nullptr,
+                         bool stale_sorted = false, uint32_t age = 0) {
     FluidInternals fi = fluid_internals(f);
     const DevBuffers& d = *fi.d;
     uint32_t e = 0;
@@ -442,8 +451,19 @@ wc_status prepare_sample(wc_surrogate* s, wc_fluid* f, bool saved) {
     if (s->has_target) gather4(n, d.perm, s->target_in, w.target_s, s->stream);
     const float k_feature = fi.params->stiffness / fi.params->rest_density * 200.0f;
     const float inv_dv = 1.0f / (s->dt * s->cfg.accel_scale);
+    const float4* stale_sorted_buf = nullptr;
+    if (stale && age > 0) {
+        if (stale_sorted) {
+            stale_sorted_buf = stale;
+        } else {
+            gather4(n, d.perm, stale, w.stale_s, s->stream);
+            stale_sorted_buf = w.stale_s;
+        }
+        if (s->has_target) sub_xyz(n, w.target_s, stale_sorted_buf, s->stream);
+    }
+    s->has_stale = stale_sorted_buf != nullptr && !stale_sorted;
     node_features(n, d.pos_b, w.hist_s, 1.0f / s->cfg.velocity_scale, inv_dv, 1.0f / fi.sc->h, fi.sc->size, k_feature,
-                  w.xn, s->stream);
+                  stale_sorted_buf, 1.0f / s->cfg.accel_scale, (float)age * 0.125f, w.xn, s->stream);
     edge_features(e, d.pos_b, w.recv, w.col, 1.0f / fi.sc->h, w.xe, s->stream);
     s->n = n;
     s->e = e;
@@ -576,8 +596,10 @@ wc_status ensure_inputs(wc_surrogate* s, uint32_t n) {
     if (n <= s->cap_in) return WC_OK;
     dfree(s->hist_in);
     dfree(s->target_in);
+    dfree(s->stale_in);
     WC_TRY(dalloc(&s->hist_in, 5 * (size_t)n));
     WC_TRY(dalloc(&s->target_in, n));
+    WC_TRY(dalloc(&s->stale_in, n));
     s->cap_in = n;
     return WC_OK;
 }
@@ -649,6 +671,7 @@ struct RolloutRun {
     wc_rollout_stats* out;
     const float* host_hist;  // initial velocity history, or null
     LaunchDims dims{};
+    uint32_t age = 0;  // steps since the SPH acceleration in s->stale was computed
     double err_sum = 0.0, err_max = 0.0;
 
     wc_status copy(float4* dst, const float4* src) {
@@ -664,12 +687,25 @@ struct RolloutRun {
         const float* acc;
         uint32_t ld;
         float scale;
-        if (mode == WC_ROLLOUT_SURROGATE) {
-            WC_TRY(prepare_sample(s, f, false));
-            WC_TRY(forward(s));
-            acc = s->work.out;
-            ld = OUT;
-            scale = s->cfg.accel_scale;
+        if (mode == WC_ROLLOUT_SURROGATE || mode == WC_ROLLOUT_HYBRID) {
+            if (mode == WC_ROLLOUT_HYBRID) {
+                // the last SPH acceleration, in this step's sorted order, as network input; the
+                // step's acceleration is that plus the network's residual (work.stale_s is free
+                // in a rollout: the stale input is already sorted)
+                gather4(D.n, D.perm, s->stale, s->stale_tmp, fi.stream);
+                WC_TRY(prepare_sample(s, f, false, s->stale_tmp, true, age));
+                WC_TRY(forward(s));
+                add_scaled(D.n, s->work.out, OUT, s->cfg.accel_scale, s->stale_tmp, s->work.stale_s, fi.stream);
+                acc = reinterpret_cast<const float*>(s->work.stale_s);
+                ld = 4;
+                scale = 1.0f;
+            } else {
+                WC_TRY(prepare_sample(s, f, false));
+                WC_TRY(forward(s));
+                acc = s->work.out;
+                ld = OUT;
+                scale = s->cfg.accel_scale;
+            }
         } else {
             gather4(D.n, D.perm, s->stale, s->stale_tmp, fi.stream);
             acc = reinterpret_cast<const float*>(s->stale_tmp);
@@ -705,7 +741,7 @@ struct RolloutRun {
         const uint32_t n = D.n;
         WC_TRY(candidate(s->alt_pos, s->alt_vel));  // the state buffer is left as it was
         WC_TRY(fluid_graph_step(f, dt));             // SPH next state, in the same sorted order
-        if (mode == WC_ROLLOUT_STALE) WC_TRY(copy(s->stale, D.accel));
+        if (mode != WC_ROLLOUT_SURROGATE) WC_TRY(copy(s->stale, D.accel));
         WC_TRY(copy(s->save_pos, D.pos_a));
         WC_TRY(copy(s->save_vel, D.vel_a));
         densities(s->rho_a);
@@ -732,7 +768,8 @@ struct RolloutRun {
         } else {
             ++out->surrogate_steps;
         }
-        if (mode == WC_ROLLOUT_SURROGATE) shift_history();
+        if (mode != WC_ROLLOUT_STALE) shift_history();
+        age = 1;  // the judge's SPH acceleration is the one the next step sees
         return WC_OK;
     }
 
@@ -757,17 +794,28 @@ struct RolloutRun {
         cudaEventRecord(e0, fi.stream);
         wc_status rc = WC_OK;
         for (uint32_t step = 0; step < nsteps && rc == WC_OK; ++step) {
-            if (mode == WC_ROLLOUT_STALE && step == 0) {
+            if (mode != WC_ROLLOUT_SURROGATE && step == 0) {
                 // no SPH acceleration yet: one plain step records it
                 rc = fluid_graph_step(f, dt);
                 if (rc == WC_OK) rc = copy(s->stale, D.accel);
+                if (rc == WC_OK && mode == WC_ROLLOUT_HYBRID) {
+                    // the history gains the step's velocity in its order (the sort's permutation)
+                    rc = ensure_work(s, D.n, std::max(s->work.cap_e, 1u), false);
+                }
+                if (rc == WC_OK && mode == WC_ROLLOUT_HYBRID) {
+                    for (int k = 0; k < 4; ++k)
+                        gather4(D.n, D.perm, s->hist_in + (size_t)k * D.n, s->work.hist_s + (size_t)k * D.n, fi.stream);
+                    shift_history();
+                }
+                age = 1;
                 ++out->sph_steps;
             } else if (step % K == 0) {
                 rc = judge_step();
             } else {
                 rc = candidate(D.pos_a, D.vel_a);
-                if (mode == WC_ROLLOUT_STALE) std::swap(s->stale, s->stale_tmp);
-                else if (rc == WC_OK) shift_history();
+                if (mode != WC_ROLLOUT_SURROGATE) std::swap(s->stale, s->stale_tmp);
+                if (rc == WC_OK && mode != WC_ROLLOUT_STALE) shift_history();
+                ++age;
                 ++out->surrogate_steps;
             }
             fluid_count_step(f);
@@ -868,7 +916,7 @@ WC_API void wc_surrogate_destroy(wc_surrogate* s) {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_work(s->work);
-    void* ptrs[] = {s->w, s->g, s->m, s->v, s->wb, s->d_err, s->hist_in, s->target_in, s->save_pos, s->save_vel,
+    void* ptrs[] = {s->w, s->g, s->m, s->v, s->wb, s->d_err, s->hist_in, s->target_in, s->stale_in, s->save_pos, s->save_vel,
                     s->alt_pos, s->alt_vel, s->stale, s->stale_tmp, s->rho_a, s->rho_b, s->err_part};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -914,7 +962,7 @@ WC_API wc_status wc_surrogate_zero_grads(wc_surrogate* s) {
 }
 
 WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, const float* host_hist,
-                                     const float* host_target) {
+                                     const float* host_target, const float* host_stale, uint32_t stale_age) {
     clear_error();
     WC_NVTX("wc_surrogate_sample");
     if (!s || !f || !host_hist) return fail(WC_ERR_INVALID_ARG, "null argument");
@@ -929,10 +977,13 @@ WC_API wc_status wc_surrogate_sample(wc_surrogate* s, wc_fluid* f, float dt, con
     s->has_target = host_target != nullptr;
     if (host_target)
         WC_CUDA_TRY(cudaMemcpyAsync(s->target_in, host_target, sizeof(float4) * n, cudaMemcpyHostToDevice, s->stream));
+    const bool stale = host_stale != nullptr && stale_age > 0;
+    if (stale)
+        WC_CUDA_TRY(cudaMemcpyAsync(s->stale_in, host_stale, sizeof(float4) * n, cudaMemcpyHostToDevice, s->stream));
     WC_CUDA_TRY(cudaStreamSynchronize(s->stream));
     fluid_enqueue_sort(f);
     WC_CUDA_TRY(cudaStreamSynchronize(fi.stream));
-    WC_TRY(prepare_sample(s, f, true));
+    WC_TRY(prepare_sample(s, f, true, stale ? s->stale_in : nullptr, false, stale ? stale_age : 0u));
     s->fluid = f;
     return read_err(s);
 }
@@ -969,12 +1020,18 @@ WC_API wc_status wc_surrogate_predictions(wc_surrogate* s, float* host_out, uint
     FluidInternals fi = fluid_internals(s->fluid);
     std::vector<float> out((size_t)n * OUT);
     std::vector<uint32_t> perm(n);
+    std::vector<float4> base(s->has_stale ? n : 0);
     WC_CUDA_TRY(cudaMemcpyAsync(out.data(), s->work.out, sizeof(float) * out.size(), cudaMemcpyDeviceToHost, s->stream));
     WC_CUDA_TRY(cudaMemcpyAsync(perm.data(), fi.d->perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s->stream));
+    if (s->has_stale)
+        WC_CUDA_TRY(cudaMemcpyAsync(base.data(), s->work.stale_s, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
     WC_TRY(read_err(s));
-    for (uint32_t k = 0; k < n; ++k)
+    for (uint32_t k = 0; k < n; ++k) {
+        const float b[3] = {s->has_stale ? base[k].x : 0.f, s->has_stale ? base[k].y : 0.f,
+                            s->has_stale ? base[k].z : 0.f};
         for (int a = 0; a < 4; ++a)
-            host_out[(size_t)perm[k] * 4 + a] = a < 3 ? out[(size_t)k * OUT + a] * s->cfg.accel_scale : 0.f;
+            host_out[(size_t)perm[k] * 4 + a] = a < 3 ? std::fmaf(out[(size_t)k * OUT + a], s->cfg.accel_scale, b[a]) : 0.f;
+    }
     return WC_OK;
 }
 
@@ -996,7 +1053,8 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
     if (!out) return fail(WC_ERR_INVALID_ARG, "null argument");
     std::memset(out, 0, sizeof *out);
     if (!f || (mode != WC_ROLLOUT_SPH && !s)) return fail(WC_ERR_INVALID_ARG, "null argument");
-    if (mode != WC_ROLLOUT_SPH && mode != WC_ROLLOUT_SURROGATE && mode != WC_ROLLOUT_STALE)
+    if (mode != WC_ROLLOUT_SPH && mode != WC_ROLLOUT_SURROGATE && mode != WC_ROLLOUT_STALE &&
+        mode != WC_ROLLOUT_HYBRID)
         return fail(WC_ERR_INVALID_ARG, "unknown rollout mode %d", mode);
     if (K == 0) return fail(WC_ERR_INVALID_ARG, "K must be >= 1");
     if (mode == WC_ROLLOUT_SPH) {
@@ -1051,7 +1109,8 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
         s->cap_roll = n;
     }
     const bool was_recording = fi.d->accel != nullptr;
-    if (mode == WC_ROLLOUT_STALE && !was_recording) WC_TRY(wc_fluid_set_recording(f, 1));
+    const bool needs_accel = mode == WC_ROLLOUT_STALE || mode == WC_ROLLOUT_HYBRID;
+    if (needs_accel && !was_recording) WC_TRY(wc_fluid_set_recording(f, 1));
     WC_CUDA_TRY(cudaStreamSynchronize(fi.stream));
     WC_TRY(fluid_diag(f, out->diag_start));
     cudaStream_t own = s->stream;
@@ -1061,7 +1120,7 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
     const wc_status rc = run.go(nsteps);
     s->stream = own;
     s->fluid = nullptr;  // the loaded sample was replaced by the rollout's graphs
-    if (mode == WC_ROLLOUT_STALE && !was_recording) wc_fluid_set_recording(f, 0);
+    if (needs_accel && !was_recording) wc_fluid_set_recording(f, 0);
     if (rc != WC_OK) return rc;
     WC_TRY(read_err(s));
     return fluid_diag(f, out->diag_end);

@@ -21,6 +21,7 @@ from .fluid import Fluid
 WC_ROLLOUT_SPH = 0
 WC_ROLLOUT_SURROGATE = 1
 WC_ROLLOUT_STALE = 2
+WC_ROLLOUT_HYBRID = 3
 HISTORY = 5  # velocities per node feature (current + 4 previous)
 
 
@@ -63,9 +64,11 @@ class Surrogate:
         check(lib().wc_surrogate_zero_grads(self._h), "zero_grads")
 
     # ---- one sample ----------------------------------------------------------------------------
-    def sample(self, fluid: Fluid, dt: float, hist: np.ndarray, target: np.ndarray | None = None) -> None:
+    def sample(self, fluid: Fluid, dt: float, hist: np.ndarray, target: np.ndarray | None = None,
+               stale: np.ndarray | None = None, stale_age: int = 0) -> None:
         """Load the fluid's current particles with their velocity history hist (5, n, 4), steps
-        dt apart, and optional target accelerations (n, 4), both in the fluid's state order."""
+        dt apart, optional target accelerations (n, 4) and optionally the last SPH acceleration
+        (n, 4) computed stale_age >= 1 steps earlier, all in the fluid's state order."""
         n = fluid.numParticles()
         hist = np.ascontiguousarray(hist, dtype=np.float32)
         if hist.shape != (HISTORY, n, 4):
@@ -76,7 +79,16 @@ class Surrogate:
             if target.shape != (n, 4):
                 raise A.WatercubeError(A.WC_ERR_INVALID_ARG, f"target has shape {target.shape}")
             tp = A._ptr(target)
-        check(lib().wc_surrogate_sample(self._h, fluid._require(), float(dt), A._ptr(hist), tp), "wc_surrogate_sample")
+        sp = None
+        if stale is not None and stale_age > 0:
+            stale = np.ascontiguousarray(stale, dtype=np.float32)
+            if stale.shape != (n, 4):
+                raise A.WatercubeError(A.WC_ERR_INVALID_ARG, f"stale acceleration has shape {stale.shape}")
+            sp = A._ptr(stale)
+        else:
+            stale_age = 0
+        check(lib().wc_surrogate_sample(self._h, fluid._require(), float(dt), A._ptr(hist), tp, sp, int(stale_age)),
+              "wc_surrogate_sample")
         self._n = n
 
     def forward_backward(self, backward: bool = True) -> float:
@@ -191,10 +203,16 @@ def record_samples(specs, steps: int, dt: float, every: int = 1, start: int = 0,
 
 class Trainer:
     """Adam on batches of samples (gradients accumulated over the batch, averaged), one
-    wc_fluid per scene holding the sample's particles for the graph build."""
+    wc_fluid per scene holding the sample's particles for the graph build.
+
+    The hybrid rollout feeds the network the last SPH acceleration and its age. Training shows
+    it the same: for each sample, with probability 1 - p_no_stale, the target of the same
+    scene k steps earlier (k uniform in 1 .. stale_k_max, when recorded) with age k, which makes
+    the sample residual (the network learns the change since then); otherwise none, as the plain
+    surrogate rollout runs."""
 
     def __init__(self, surrogate: Surrogate, params: list, position_noise: float = 3e-4, seed: int = 0,
-                 velocity_noise: float = 0.0):
+                 velocity_noise: float = 0.0, p_no_stale: float = 0.2, stale_k_max: int = 7):
         self.s = surrogate
         self.params = params
         self.noise = position_noise
@@ -202,7 +220,27 @@ class Trainer:
         # hist[0] and moves with it): robustness to the network's own past errors in a rollout
         self.vnoise = velocity_noise
         self.rng = np.random.default_rng(seed)
+        self.p_no_stale = p_no_stale
+        self.stale_k_max = stale_k_max
+        self.by: dict[tuple[int, int], Sample] = {}
         self._fluids: dict[int, Fluid] = {}
+
+    def index(self, samples: list[Sample]) -> None:
+        """Make `samples` available as the source of earlier SPH accelerations."""
+        for x in samples:
+            self.by[(x.scene, x.step)] = x
+
+    def stale_for(self, smp: Sample, k: int) -> np.ndarray | None:
+        """The SPH acceleration of the same scene k steps before smp, if recorded."""
+        src = self.by.get((smp.scene, smp.step - k)) if k > 0 else None
+        return None if src is None else src.target
+
+    def draw_stale(self, smp: Sample) -> tuple[np.ndarray | None, int]:
+        if self.stale_k_max < 1 or self.rng.random() < self.p_no_stale:
+            return None, 0
+        k = int(self.rng.integers(1, self.stale_k_max + 1))
+        st = self.stale_for(smp, k)
+        return (st, k) if st is not None else (None, 0)
 
     def fluid(self, scene: int, state: np.ndarray) -> Fluid:
         f = self._fluids.get(scene)
@@ -214,8 +252,16 @@ class Trainer:
             f.set_particles(state)
         return f
 
-    def load(self, smp: Sample, noise: bool) -> None:
+    def load(self, smp: Sample, noise: bool, stale_k: int | None = None) -> None:
+        """Load smp; stale_k None draws the stale acceleration at random (training), an int
+        gives its age (0: none)."""
         state, hist = smp.state, smp.hist
+        if stale_k is None:
+            stale, age = self.draw_stale(smp)
+        else:
+            stale, age = self.stale_for(smp, stale_k), stale_k
+            if stale is None:
+                age = 0
         if noise and self.vnoise > 0:
             hist = hist + np.pad(self.rng.normal(0.0, self.vnoise, hist[..., :3].shape),
                                  ((0, 0), (0, 0), (0, 1))).astype(np.float32)
@@ -228,31 +274,33 @@ class Trainer:
             border = self.params[smp.scene].wall_border
             np.clip(state["position"], border, size - border, out=state["position"])
         f = self.fluid(smp.scene, state)
-        self.s.sample(f, smp.dt, hist, smp.target)
+        self.s.sample(f, smp.dt, hist, smp.target, stale, age)
 
     def step(self, batch: list[Sample], lr: float) -> float:
         """One Adam step over `batch`; returns the mean loss."""
         losses = []
         for smp in batch:
-            self.load(smp, noise=True)
+            self.load(smp, noise=True, stale_k=None)
             losses.append(self.s.forward_backward(True))
         self.s.adam(lr, 1.0 / len(batch))
         return float(np.mean(losses))
 
-    def evaluate(self, samples: list[Sample]) -> float:
-        """Mean loss over samples (no noise, no gradient)."""
+    def evaluate(self, samples: list[Sample], stale_k: int = 0) -> float:
+        """Mean loss over samples (no noise, no gradient), with the SPH acceleration of stale_k
+        steps earlier as input (0: none)."""
         out = []
         for smp in samples:
-            self.load(smp, noise=False)
+            self.load(smp, noise=False, stale_k=stale_k)
             out.append(self.s.forward_backward(False))
         return float(np.mean(out))
 
-    def predict(self, smp: Sample) -> np.ndarray:
-        self.load(smp, noise=False)
+    def predict(self, smp: Sample, stale_k: int = 0) -> np.ndarray:
+        self.load(smp, noise=False, stale_k=stale_k)
         self.s.forward_backward(False)
         return self.s.predictions()
 
     def train(self, samples: list[Sample], steps: int, lr: float = 1e-4, batch: int = 8) -> list[float]:
+        self.index(samples)
         hist = []
         for _ in range(steps):
             idx = self.rng.choice(len(samples), size=min(batch, len(samples)), replace=False)

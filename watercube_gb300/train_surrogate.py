@@ -6,10 +6,15 @@ Training data: `--scenes` random scenes (the batched workload's scene draw at sm
 counts, seed `--seed`) run by wc_batch for `--frames` steps at dt = 1e-3 with acceleration
 recording on; every frame of every scene is a sample. The last quarter of the scenes is held
 out. Adam on batches of 8 samples (lr `--lr`, then lr / 3 for the last 30% of the steps), input
-noise sigma = 3e-4 on positions. The report printed at the end (and stored in the .npz) gives
-the held-out per-step acceleration error of the network beside the method without it: the
-SPH acceleration of k steps earlier reused, as a judged rollout with interval K does for
-k = 1 .. K-1.
+noise sigma = 3e-4 on positions. Each training sample carries, with probability
+1 - `--p-no-stale`, the SPH acceleration of the same scene k steps earlier (k uniform in
+1 .. `--stale-k-max`) and its age as inputs, as the hybrid rollout gives them (such a sample
+is residual: the network learns the change of the acceleration since then); otherwise none, as
+the plain surrogate rollout runs. The report printed at the end (and stored in the .npz) gives
+the held-out per-step acceleration error of the network without that input, of the network
+given the SPH acceleration k steps old (hybrid_k), and of the method without the network: the
+SPH acceleration of k steps earlier reused (stale_k), as a judged rollout with interval K does
+for k = 1 .. K-1.
 """
 from __future__ import annotations
 
@@ -39,16 +44,30 @@ def stale_errors(samples, by, kmax: int) -> dict[int, float]:
     return out
 
 
-def network_error(trainer: Trainer, samples) -> float:
-    return float(np.mean([rel_error(trainer.predict(x), x.target) for x in samples]))
+def network_error(trainer: Trainer, samples, stale_k: int = 0) -> float:
+    """Mean relative error of the network's acceleration, given the SPH acceleration of stale_k
+    steps earlier (0: none). The trainer's index must hold the earlier samples."""
+    return float(np.mean([rel_error(trainer.predict(x, stale_k), x.target) for x in samples]))
+
+
+def hybrid_errors(trainer: Trainer, samples, by, kmax: int) -> dict[int, float]:
+    out = {}
+    for k in range(1, kmax + 1):
+        have = [x for x in samples if (x.scene, x.step - k) in by]
+        out[k] = network_error(trainer, have, k)
+    return out
 
 
 def report(trainer: Trainer, samples, by, K_values=(4, 8)) -> dict:
-    stale = stale_errors(samples, by, max(K_values) - 1)
+    kmax = max(K_values) - 1
+    trainer.index(list(by.values()))
+    stale = stale_errors(samples, by, kmax)
+    hybrid = hybrid_errors(trainer, samples, by, kmax)
     net = network_error(trainer, samples)
-    out = {"network": net, "stale_k": stale}
+    out = {"network": net, "stale_k": stale, "hybrid_k": hybrid}
     for K in K_values:
         out[f"stale_mean_K{K}"] = float(np.mean([stale[k] for k in range(1, K)]))
+        out[f"hybrid_mean_K{K}"] = float(np.mean([hybrid[k] for k in range(1, K)]))
     return out
 
 
@@ -80,6 +99,8 @@ def main(argv=None) -> dict:
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--velocity-noise", type=float, default=0.0)
+    ap.add_argument("--p-no-stale", type=float, default=0.2)
+    ap.add_argument("--stale-k-max", type=int, default=7)
     ap.add_argument("--out", type=Path, default=DEFAULT_WEIGHTS)
     args = ap.parse_args(argv)
 
@@ -93,7 +114,8 @@ def main(argv=None) -> dict:
     t_data = time.time() - t0
 
     s = Surrogate(layers=args.layers, seed=args.seed)
-    tr = Trainer(s, params, seed=args.seed, velocity_noise=args.velocity_noise)
+    tr = Trainer(s, params, seed=args.seed, velocity_noise=args.velocity_noise, p_no_stale=args.p_no_stale,
+                 stale_k_max=args.stale_k_max)
     t1 = time.time()
     losses = []
     cut = int(args.steps * 0.7)
@@ -104,6 +126,7 @@ def main(argv=None) -> dict:
     meta = {
         "scenes": args.scenes, "n_range": [args.n_min, args.n_max], "frames": args.frames, "seed": args.seed,
         "steps": args.steps, "lr": args.lr, "batch": args.batch, "velocity_noise": args.velocity_noise,
+        "p_no_stale": args.p_no_stale, "stale_k_max": args.stale_k_max,
         "held_out_scenes": list(range(held_from, args.scenes)), "train_seconds": t_train,
         "data_seconds": t_data, "final_train_loss": float(np.mean(losses[-50:])), "held_out": rep,
     }
