@@ -99,12 +99,12 @@ constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;  // ~0.3-1 s of polling before gi
 
 // SPH passes: 256-thread blocks of 8 cell teams (one warp each).
 constexpr int SPH_THREADS = 256;
-// Candidates a warp stages in shared memory per cell (plus 64 padding entries).
+// Candidates a warp stages in shared memory per cell in the density pass (padding included).
 constexpr int STAGE_CAP = 320;
 // 32-bit words of neighbour bit strings per particle (density pass -> force pass).
 constexpr int MASK_WORDS = 16;
-// Force kernel direct path: per-lane neighbour list capacity ([CAP][32] words per warp).
-constexpr int FORCE_LIST_CAP = 24;
+// Force kernel dense path: per-lane neighbour list capacity ([CAP][32] words per warp).
+constexpr int FORCE_LIST_CAP = 16;
 
 struct DevBuffers {
     uint32_t n;          // particles

@@ -40,6 +40,11 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int WARPS = SPH_THREADS / 32;
+// Force pass, dense path: candidates staged per piece, and the most slices a target takes.
+constexpr int FORCE_STAGE = 128;
+constexpr uint32_t FORCE_DENSE_SLICES = 4;
+// Force pass, replay path: neighbour-list entries per warp (the dense path's list and stage space).
+constexpr int FORCE_REPLAY_LIST = FORCE_LIST_CAP * 32 + 3 * FORCE_STAGE;
 
 // ---- packed f32x2 arithmetic (two floats in one 64-bit register; lo = first) ---------------------
 typedef unsigned long long f2;
@@ -70,10 +75,12 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
 }
 
 // Four staged candidates against one target: hit bits (bit c for candidate c) and the Poly6
-// weights (cull - d2)^3 of the hits added to acc01 / acc23.
+// weights (cull - d2)^3 of the hits added to acc01 / acc23. The stage holds CAP x values, then
+// CAP y values, then CAP z values.
+template <int CAP = STAGE_CAP>
 __device__ __forceinline__ uint32_t quad_hits(const ulonglong2* q, f2 px, f2 py, f2 pz, f2 cull2, f2& acc01,
                                               f2& acc23) {
-    const ulonglong2 X = q[0], Y = q[STAGE_CAP / 4], Z = q[STAGE_CAP / 2];
+    const ulonglong2 X = q[0], Y = q[CAP / 4], Z = q[CAP / 2];
     const f2 dx01 = sub2(px, X.x), dx23 = sub2(px, X.y);
     const f2 dy01 = sub2(py, Y.x), dy23 = sub2(py, Y.y);
     const f2 dz01 = sub2(pz, Z.x), dz23 = sub2(pz, Z.y);
@@ -90,6 +97,23 @@ __device__ __forceinline__ uint32_t quad_hits(const ulonglong2* q, f2 px, f2 py,
     const f2 w23 = pk(fmaxf(u2, 0.f), fmaxf(u3, 0.f));
     acc01 = fma2(mul2(w01, w01), w01, acc01);
     acc23 = fma2(mul2(w23, w23), w23, acc23);
+    return miss ^ 0xFu;
+}
+
+// The same test without the weights (the force pass's culling).
+template <int CAP>
+__device__ __forceinline__ uint32_t quad_test(const ulonglong2* q, f2 px, f2 py, f2 pz, f2 cull2) {
+    const ulonglong2 X = q[0], Y = q[CAP / 4], Z = q[CAP / 2];
+    const f2 dx01 = sub2(px, X.x), dx23 = sub2(px, X.y);
+    const f2 dy01 = sub2(py, Y.x), dy23 = sub2(py, Y.y);
+    const f2 dz01 = sub2(pz, Z.x), dz23 = sub2(pz, Z.y);
+    const f2 d01 = fma2(dz01, dz01, fma2(dy01, dy01, mul2(dx01, dx01)));
+    const f2 d23 = fma2(dz23, dz23, fma2(dy23, dy23, mul2(dx23, dx23)));
+    float u0, u1, u2, u3;
+    upk(sub2(cull2, d01), u0, u1);
+    upk(sub2(cull2, d23), u2, u3);
+    const uint32_t miss = (__float_as_uint(u0) >> 31) | ((__float_as_uint(u1) >> 30) & 2u) |
+                          ((__float_as_uint(u2) >> 29) & 4u) | ((__float_as_uint(u3) >> 28) & 8u);
     return miss ^ 0xFu;
 }
 
@@ -197,6 +221,40 @@ __device__ __forceinline__ uint32_t max_slices(uint32_t ncell) {
     const uint32_t rem = ncell & 31u;
     const uint32_t last = rem ? rem : 32u;
     return 32u / last;
+}
+
+// Dense path staging: candidates [c0, c0 + len) of the cell's concatenated list into a CAP-entry
+// x/y/z stage (asynchronous copies, one wait), then `pad` far-away entries after them; with
+// SLOTS, slot[j] = the sorted slot of staged candidate j. len + pad <= CAP. Callers sync the warp
+// before restaging (the previous chunk's readers must be done).
+template <int CAP, bool SLOTS>
+__device__ __forceinline__ void stage_chunk(float* sx, uint32_t* slot, const CellRows& cr, uint32_t c0, uint32_t len,
+                                            uint32_t pad, const float4* __restrict__ pos, uint32_t lane) {
+    const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(sx);
+    const uint32_t c1 = c0 + len;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
+        const uint32_t rlen = __shfl_sync(FULL, cr.len, r);
+        const uint32_t base = __shfl_sync(FULL, cr.pex, r);
+        const uint32_t a = max(base, c0), b = min(base + rlen, c1);
+        for (uint32_t j = a + lane; j < b; j += 32u) {
+            const uint32_t k = lo + (j - base);
+            const float* g = reinterpret_cast<const float*>(pos + k);
+            const uint32_t at = s0 + 4u * (j - c0);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(at), "l"(g) : "memory");
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(at + 4u * CAP), "l"(g + 1) : "memory");
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(at + 8u * CAP), "l"(g + 2) : "memory");
+            if (SLOTS) slot[j - c0] = k;
+        }
+    }
+    for (uint32_t j = lane; j < pad; j += 32u) {
+        sx[len + j] = 1e30f;
+        sx[CAP + len + j] = 1e30f;
+        sx[2 * CAP + len + j] = 1e30f;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
 }
 
 // ---- reference-only terms ---------------------------------------------------------------------
@@ -436,33 +494,42 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
             }
             __syncwarp();  // the stage is rewritten for the next cell
         } else {
-            // Direct path: candidates straight from global memory (no bit strings).
+            // Dense path (the candidate list does not fit the stage): each chunk of 32 targets
+            // streams the list through the stage in pieces and tests it as above, without bit
+            // strings (the force pass culls these cells itself).
             for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
                 const uint32_t nt = min(32u, cr.cend - t0);
                 const Team tm = make_team(nt, lane);
                 const uint32_t ti = t0 + tm.t;
                 const float4 pi = pos_in[ti];
-                float sum = 0.f;
-                uint32_t cnt = 0;
-#pragma unroll 1
-                for (int r = 0; r < 9; ++r) {
-                    const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
-                    const uint32_t hi = lo + __shfl_sync(FULL, cr.len, r);
-                    if (!tm.active) continue;
-                    for (uint32_t k = lo + tm.sl; k < hi; k += tm.S) {
-                        const float4 pj = __ldg(pos_in + k);
-                        const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
-                        if (d2 <= sc.cull) {
-                            const float w = sc.h2 - d2;
-                            sum = fmaf(w * w, w, sum);
-                            ++cnt;
-                        }
-                    }
+                const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
+                const uint32_t tpad = stage_padding(tm.S);
+                const uint32_t chunk = (uint32_t)STAGE_CAP - tpad;  // a multiple of 4, >= 184
+                f2 acc01 = 0ull, acc23 = 0ull;
+                uint32_t nh = 0;
+                for (uint32_t c0 = 0; c0 < cr.total; c0 += chunk) {
+                    const uint32_t len = min(chunk, cr.total - c0);
+                    __syncwarp();  // the previous piece's readers are done
+                    stage_chunk<STAGE_CAP, false>(sx, nullptr, cr, c0, len, tpad, pos_in, lane);
+                    const uint32_t IT = (((len + 3u) >> 2) + tm.S - 1u) / tm.S;
+                    const ulonglong2* qx = reinterpret_cast<const ulonglong2*>(sx) + tm.sl;
+#pragma unroll 4
+                    for (uint32_t j = 0; j < IT; ++j, qx += tm.S)
+                        nh += __popc(quad_hits(qx, px, py, pz, cull2, acc01, acc23));
+                }
+                float a0, a1, a2, a3;
+                upk(acc01, a0, a1);
+                upk(acc23, a2, a3);
+                float sum = (a0 + a1) + (a2 + a3);
+                if (!tm.active) {
+                    sum = 0.f;
+                    nh = 0;
                 }
                 sum = slice_sum(sum, tm.S, nt, tm.sl);
-                cnt = slice_sum(cnt, tm.S, nt, tm.sl);
-                if (tm.sl == 0u) write_density(sc, sum, cnt, pi, ti, rho_out, p_out, ncount);
+                nh = slice_sum(nh, tm.S, nt, tm.sl);
+                if (tm.sl == 0u) write_density(sc, sum, nh, pi, ti, rho_out, p_out, ncount);
             }
+            __syncwarp();  // the stage is rewritten for the next cell
         }
     }
 }
@@ -567,16 +634,18 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                                                                const uint32_t* __restrict__ hits,
                                                                float4* __restrict__ accel,
                                                                uint32_t* __restrict__ err) {
-    __shared__ uint32_t s_slot[WARPS][STAGE_CAP];             // candidate number -> sorted slot
-    __shared__ uint32_t s_lists[WARPS][FORCE_LIST_CAP * 32];  // direct path: per-lane lists
+    // Per warp: the slot table (candidate number -> sorted slot), then the dense path's per-lane
+    // lists and its x/y/z stage; the replay path's neighbour lists use both of those regions.
+    __shared__ __align__(16) uint32_t s_work[WARPS][STAGE_CAP + FORCE_REPLAY_LIST];
     __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
     if (BATCHED) {
         for (uint32_t t = threadIdx.x; t <= bt.num_scenes; t += blockDim.x) s_coff[t] = bt.coff[t];
         __syncthreads();
     }
     const uint32_t lane = threadIdx.x & 31u;
-    uint32_t* slot = s_slot[threadIdx.x >> 5];
-    uint32_t* list = s_lists[threadIdx.x >> 5];
+    uint32_t* slot = s_work[threadIdx.x >> 5];
+    uint32_t* list = slot + STAGE_CAP;
+    float* fx = reinterpret_cast<float*>(list + FORCE_LIST_CAP * 32);
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t M = min(*num_nonempty, num_cells);
@@ -646,7 +715,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
             }
             const uint32_t all = __shfl_sync(FULL, tinc, 31);
             const uint32_t seg = __shfl_sync(FULL, tinc - tv, tm.t);
-            if (all <= (uint32_t)(FORCE_LIST_CAP * 32)) {
+            if (all <= (uint32_t)FORCE_REPLAY_LIST) {
                 // Decode the bits once into the target's list segment ...
                 if (tm.active) {
                     uint32_t at = seg + inc - cnt;
@@ -732,37 +801,48 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
             __syncwarp();  // the slot table is rewritten for the next cell
             continue;
         }
-        // Direct path: cull every candidate into per-lane shared-memory lists, then evaluate.
+        // Dense path (no bit strings for this cell): each chunk of 32 targets streams its
+        // candidate list through the small stage in pieces, culls it with the packed test into
+        // per-lane lists of sorted slots, and evaluates a list whenever it could overflow. At
+        // most FORCE_DENSE_SLICES slices per target, so a piece keeps most of the stage.
+        const f2 cull2 = pk(sc.cull, sc.cull);
         for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
             const uint32_t nt = min(32u, cr.cend - t0);
-            const Team tm = make_team(nt, lane);
+            Team tm = make_team(nt, lane);
+            if (tm.S > FORCE_DENSE_SLICES) {
+                tm.S = FORCE_DENSE_SLICES;
+                tm.active = tm.sl < tm.S;
+            }
             const uint32_t ti = t0 + tm.t;
             const float4 pi = pos_b[ti];
             const float4 vi = vel_b[ti];
+            const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
+            const uint32_t tpad = stage_padding(tm.S);
+            const uint32_t chunk = (uint32_t)FORCE_STAGE - tpad;  // a multiple of 4, >= 104
+            const uint32_t rsl = tm.active ? tm.sl : 0u;          // idle lanes read slice 0, keep nothing
             float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             uint32_t cnt = 0;
-#pragma unroll 1
-            for (int r = 0; r < 9; ++r) {
-                const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
-                const uint32_t hi = lo + __shfl_sync(FULL, cr.len, r);
-                const uint32_t iters = (hi - lo + tm.S - 1u) / tm.S;
-                for (uint32_t seg = 0; seg < iters; seg += FORCE_LIST_CAP) {
-                    const uint32_t seg_iters = min((uint32_t)FORCE_LIST_CAP, iters - seg);
-                    if (__any_sync(FULL, cnt + seg_iters > (uint32_t)FORCE_LIST_CAP)) {
+            for (uint32_t c0 = 0; c0 < cr.total; c0 += chunk) {
+                const uint32_t len = min(chunk, cr.total - c0);
+                __syncwarp();  // the previous piece's readers are done
+                stage_chunk<FORCE_STAGE, true>(fx, slot, cr, c0, len, tpad, pos_b, lane);
+                const uint32_t IT = (((len + 3u) >> 2) + tm.S - 1u) / tm.S;
+                const ulonglong2* qx = reinterpret_cast<const ulonglong2*>(fx) + rsl;
+                for (uint32_t j = 0; j < IT; ++j, qx += tm.S) {
+                    if (__any_sync(FULL, cnt + 4u > (uint32_t)FORCE_LIST_CAP)) {
                         accumulate_list(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
                         cnt = 0;
                     }
-                    if (tm.active) {
-                        const uint32_t k0 = lo + seg * tm.S + tm.sl;
-                        for (uint32_t it = 0; it < seg_iters; ++it) {
-                            const uint32_t k = k0 + it * tm.S;
-                            if (k < hi) {
-                                const float4 pj = __ldg(pos_b + k);
-                                const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
-                                // The particle itself passes too; it contributes exactly zero.
-                                if (d2 <= sc.cull) list[(cnt++) * 32u + lane] = k;
-                            }
-                        }
+                    uint32_t bits = quad_test<FORCE_STAGE>(qx, px, py, pz, cull2);
+                    if (!tm.active) bits = 0u;
+                    const uint32_t qb = 4u * (rsl + j * tm.S);
+                    while (bits) {
+                        const uint32_t b = (uint32_t)__ffs(bits) - 1u;
+                        bits &= bits - 1u;
+                        const uint32_t q = qb + b;
+                        // The particle itself passes too; it contributes exactly zero. Padding
+                        // entries never pass; the check only keeps the read inside the piece.
+                        list[(cnt++) * 32u + lane] = q < len ? slot[q] : ti;
                     }
                 }
             }
@@ -771,6 +851,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
             for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
             if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
         }
+        __syncwarp();  // the slot table and stage are rewritten for the next cell
     }
 }
 
