@@ -45,6 +45,8 @@ constexpr int FORCE_STAGE = 128;
 constexpr uint32_t FORCE_DENSE_SLICES = 4;
 // Force pass, replay path: neighbour-list entries per warp (the dense path's list and stage space).
 constexpr int FORCE_REPLAY_LIST = FORCE_LIST_CAP * 32 + 3 * FORCE_STAGE;
+// Force pass, piecewise replay: per-lane list capacity (the same space split by lane).
+constexpr int REPLAY_LANE_CAP = FORCE_REPLAY_LIST / 32;
 
 // ---- packed f32x2 arithmetic (two floats in one 64-bit register; lo = first) ---------------------
 typedef unsigned long long f2;
@@ -216,11 +218,35 @@ __device__ __forceinline__ MaskShape mask_shape(uint32_t total, uint32_t S, bool
     return ms;
 }
 
+// Bit strings of a chunk of targets split S ways over L candidates are kept (in any path) when
+// every slice's words fit the particle's slot and S <= 8, so that a word's 32 S candidates
+// lie within one slot-table piece of the force pass. Both passes decide with this test.
+__device__ __forceinline__ bool bits_fit(uint32_t L, uint32_t S) {
+    const uint32_t IT = (((L + 3u) >> 2) + S - 1u) / S;
+    const uint32_t nwords = (IT + 7u) >> 3;
+    return S <= 8u && nwords * S <= (uint32_t)MASK_WORDS;
+}
+
 // The split of the last (smallest) chunk of a cell has the most slices, hence the most padding.
 __device__ __forceinline__ uint32_t max_slices(uint32_t ncell) {
     const uint32_t rem = ncell & 31u;
     const uint32_t last = rem ? rem : 32u;
     return 32u / last;
+}
+
+// slot[j] = the sorted slot of candidate c0 + j of the cell's concatenated list, j < len.
+__device__ __forceinline__ void fill_slots(uint32_t* slot, const CellRows& cr, uint32_t c0, uint32_t len,
+                                           uint32_t lane) {
+    const uint32_t c1 = c0 + len;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const uint32_t lo = __shfl_sync(FULL, cr.lo, r);
+        const uint32_t rlen = __shfl_sync(FULL, cr.len, r);
+        const uint32_t base = __shfl_sync(FULL, cr.pex, r);
+        const uint32_t a = max(base, c0), b = min(base + rlen, c1);
+        for (uint32_t j = a + lane; j < b; j += 32u) slot[j - c0] = lo + (j - base);
+    }
+    __syncwarp();
 }
 
 // Dense path staging: candidates [c0, c0 + len) of the cell's concatenated list into a CAP-entry
@@ -456,7 +482,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
                 const uint32_t nt = min(32u, cr.cend - t0);
                 const Team tm = make_team(nt, lane);
                 const MaskShape ms = mask_shape(cr.total, tm.S, single);
-                const bool store = ms.ok && hits != nullptr && tm.active;
+                const bool store = (ms.ok || bits_fit(cr.total, tm.S)) && hits != nullptr && tm.active;
                 const uint32_t ti = t0 + tm.t;
                 const float4 pi = pos_in[ti];
                 const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
@@ -495,8 +521,9 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
             __syncwarp();  // the stage is rewritten for the next cell
         } else {
             // Dense path (the candidate list does not fit the stage): each chunk of 32 targets
-            // streams the list through the stage in pieces and tests it as above, without bit
-            // strings (the force pass culls these cells itself).
+            // streams the list through the stage in pieces and tests it as above. Bit strings
+            // are kept when bits_fit: the pieces are then whole words long (32 S candidates a
+            // word), so their words form the layout one stage would have given.
             for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
                 const uint32_t nt = min(32u, cr.cend - t0);
                 const Team tm = make_team(nt, lane);
@@ -504,18 +531,40 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
                 const float4 pi = pos_in[ti];
                 const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
                 const uint32_t tpad = stage_padding(tm.S);
-                const uint32_t chunk = (uint32_t)STAGE_CAP - tpad;  // a multiple of 4, >= 184
+                const bool keep = hits != nullptr && bits_fit(cr.total, tm.S);
+                const uint32_t room = (uint32_t)STAGE_CAP - tpad;  // a multiple of 4, >= 184
+                const uint32_t chunk = keep ? 32u * tm.S * (room / (32u * tm.S)) : room;  // S <= 8: >= 256
                 f2 acc01 = 0ull, acc23 = 0ull;
-                uint32_t nh = 0;
+                uint32_t nh = 0, wbase = 0;
                 for (uint32_t c0 = 0; c0 < cr.total; c0 += chunk) {
                     const uint32_t len = min(chunk, cr.total - c0);
                     __syncwarp();  // the previous piece's readers are done
                     stage_chunk<STAGE_CAP, false>(sx, nullptr, cr, c0, len, tpad, pos_in, lane);
                     const uint32_t IT = (((len + 3u) >> 2) + tm.S - 1u) / tm.S;
                     const ulonglong2* qx = reinterpret_cast<const ulonglong2*>(sx) + tm.sl;
+                    if (keep) {
+                        const uint32_t nw = (IT + 7u) >> 3;
+                        for (uint32_t w = 0; w < nw; ++w) {
+                            uint32_t word = 0;
+                            const uint32_t jend = min(8u, IT - 8u * w);
+                            if (jend == 8u) {
+#pragma unroll
+                                for (uint32_t j = 0; j < 8u; ++j, qx += tm.S)
+                                    word |= quad_hits(qx, px, py, pz, cull2, acc01, acc23) << (4u * j);
+                            } else {
+#pragma unroll 1
+                                for (uint32_t j = 0; j < jend; ++j, qx += tm.S)
+                                    word |= quad_hits(qx, px, py, pz, cull2, acc01, acc23) << (4u * j);
+                            }
+                            nh += __popc(word);
+                            if (tm.active) hits[(size_t)ti * MASK_WORDS + (wbase + w) * tm.S + tm.sl] = word;
+                        }
+                        wbase += nw;
+                    } else {
 #pragma unroll 4
-                    for (uint32_t j = 0; j < IT; ++j, qx += tm.S)
-                        nh += __popc(quad_hits(qx, px, py, pz, cull2, acc01, acc23));
+                        for (uint32_t j = 0; j < IT; ++j, qx += tm.S)
+                            nh += __popc(quad_hits(qx, px, py, pz, cull2, acc01, acc23));
+                    }
                 }
                 float a0, a1, a2, a3;
                 upk(acc01, a0, a1);
@@ -559,12 +608,23 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
     f[5] = fmaf(vj.z - vi.z, wv, f[5]);
 }
 
-__device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t cnt, uint32_t lane, const float4& pi,
-                                                const float4& vi, const float4* __restrict__ pos,
+// A lane's list (entries list[e * 32 + lane], e < cnt), four entries per round so their loads
+// overlap; an empty place takes the particle itself (slot self), whose terms are exactly zero.
+__device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t cnt, uint32_t lane, uint32_t self,
+                                                const float4& pi, const float4& vi, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vel, float h, float f[6]) {
-    for (uint32_t e = 0; e < cnt; ++e) {
-        const uint32_t k = list[e * 32u + lane];
-        pair_terms(pi, vi, __ldg(pos + k), __ldg(vel + k), h, f);
+    for (uint32_t e = 0; e < cnt; e += 4u) {
+        uint32_t k[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) k[u] = e + (uint32_t)u < cnt ? list[(e + (uint32_t)u) * 32u + lane] : self;
+        float4 pj[4], vj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            pj[u] = __ldg(pos + k[u]);
+            vj[u] = __ldg(vel + k[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) pair_terms(pi, vi, pj[u], vj[u], h, f);
     }
 }
 
@@ -801,52 +861,86 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
             __syncwarp();  // the slot table is rewritten for the next cell
             continue;
         }
-        // Dense path (no bit strings for this cell): each chunk of 32 targets streams its
-        // candidate list through the small stage in pieces, culls it with the packed test into
-        // per-lane lists of sorted slots, and evaluates a list whenever it could overflow. At
-        // most FORCE_DENSE_SLICES slices per target, so a piece keeps most of the stage.
+        // Chunks of 32 targets. Where the density pass kept bit strings (bits_fit), they are
+        // replayed piece by piece: a slot table for the candidates of a few words, each lane
+        // decoding its words into its own list, evaluated whenever a list fills. Otherwise the
+        // dense path culls: the candidate list streams through the small stage in pieces, the
+        // packed test fills the per-lane lists (at most FORCE_DENSE_SLICES slices per target,
+        // so a piece keeps most of the stage).
         const f2 cull2 = pk(sc.cull, sc.cull);
         for (uint32_t t0 = cr.cbeg; t0 < cr.cend; t0 += 32u) {
             const uint32_t nt = min(32u, cr.cend - t0);
             Team tm = make_team(nt, lane);
-            if (tm.S > FORCE_DENSE_SLICES) {
-                tm.S = FORCE_DENSE_SLICES;
-                tm.active = tm.sl < tm.S;
-            }
             const uint32_t ti = t0 + tm.t;
             const float4 pi = pos_b[ti];
             const float4 vi = vel_b[ti];
-            const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
-            const uint32_t tpad = stage_padding(tm.S);
-            const uint32_t chunk = (uint32_t)FORCE_STAGE - tpad;  // a multiple of 4, >= 104
-            const uint32_t rsl = tm.active ? tm.sl : 0u;          // idle lanes read slice 0, keep nothing
             float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             uint32_t cnt = 0;
-            for (uint32_t c0 = 0; c0 < cr.total; c0 += chunk) {
-                const uint32_t len = min(chunk, cr.total - c0);
-                __syncwarp();  // the previous piece's readers are done
-                stage_chunk<FORCE_STAGE, true>(fx, slot, cr, c0, len, tpad, pos_b, lane);
-                const uint32_t IT = (((len + 3u) >> 2) + tm.S - 1u) / tm.S;
-                const ulonglong2* qx = reinterpret_cast<const ulonglong2*>(fx) + rsl;
-                for (uint32_t j = 0; j < IT; ++j, qx += tm.S) {
-                    if (__any_sync(FULL, cnt + 4u > (uint32_t)FORCE_LIST_CAP)) {
-                        accumulate_list(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
-                        cnt = 0;
+            if (hits != nullptr && bits_fit(cr.total, tm.S)) {
+                const uint32_t IT = (((cr.total + 3u) >> 2) + tm.S - 1u) / tm.S;
+                const uint32_t nwords = (IT + 7u) >> 3;
+                const uint32_t span = 32u * tm.S;                    // candidates per word
+                const uint32_t wpp = (uint32_t)STAGE_CAP / span;      // words per piece, >= 1
+                for (uint32_t v0 = 0; v0 < nwords; v0 += wpp) {
+                    const uint32_t c0 = v0 * span;
+                    const uint32_t len = min(wpp * span, cr.total - c0);
+                    __syncwarp();  // the previous piece's readers are done
+                    fill_slots(slot, cr, c0, len, lane);
+                    const uint32_t v1 = min(v0 + wpp, nwords);
+                    for (uint32_t v = v0; v < v1; ++v) {
+                        uint32_t word = tm.active ? __ldg(hits + (size_t)ti * MASK_WORDS + v * tm.S + tm.sl) : 0u;
+                        const uint32_t qb = 4u * (8u * v * tm.S + tm.sl) - c0;  // first candidate, in the piece
+                        for (;;) {
+                            while (word && cnt < (uint32_t)REPLAY_LANE_CAP) {
+                                const uint32_t b = (uint32_t)__ffs(word) - 1u;
+                                word &= word - 1u;
+                                const uint32_t q = qb + (b >> 2) * 4u * tm.S + (b & 3u);
+                                // Bits always come from this step's density pass over the same
+                                // tables; the check only keeps a stage-by-stage caller's stale
+                                // bits in bounds (the particle itself contributes exactly zero).
+                                list[(cnt++) * 32u + lane] = q < len ? slot[q] : ti;
+                            }
+                            if (!__any_sync(FULL, word != 0u)) break;
+                            accumulate_list(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, f);
+                            cnt = 0;
+                        }
                     }
-                    uint32_t bits = quad_test<FORCE_STAGE>(qx, px, py, pz, cull2);
-                    if (!tm.active) bits = 0u;
-                    const uint32_t qb = 4u * (rsl + j * tm.S);
-                    while (bits) {
-                        const uint32_t b = (uint32_t)__ffs(bits) - 1u;
-                        bits &= bits - 1u;
-                        const uint32_t q = qb + b;
-                        // The particle itself passes too; it contributes exactly zero. Padding
-                        // entries never pass; the check only keeps the read inside the piece.
-                        list[(cnt++) * 32u + lane] = q < len ? slot[q] : ti;
+                }
+            } else {
+                if (tm.S > FORCE_DENSE_SLICES) {
+                    tm.S = FORCE_DENSE_SLICES;
+                    tm.active = tm.sl < tm.S;
+                }
+                const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z);
+                const uint32_t tpad = stage_padding(tm.S);
+                const uint32_t chunk = (uint32_t)FORCE_STAGE - tpad;  // a multiple of 4, >= 104
+                const uint32_t rsl = tm.active ? tm.sl : 0u;          // idle lanes read slice 0, keep nothing
+                for (uint32_t c0 = 0; c0 < cr.total; c0 += chunk) {
+                    const uint32_t len = min(chunk, cr.total - c0);
+                    __syncwarp();  // the previous piece's readers are done
+                    stage_chunk<FORCE_STAGE, true>(fx, slot, cr, c0, len, tpad, pos_b, lane);
+                    const uint32_t IT = (((len + 3u) >> 2) + tm.S - 1u) / tm.S;
+                    const ulonglong2* qx = reinterpret_cast<const ulonglong2*>(fx) + rsl;
+                    for (uint32_t j = 0; j < IT; ++j, qx += tm.S) {
+                        if (__any_sync(FULL, cnt + 4u > (uint32_t)FORCE_LIST_CAP)) {
+                            accumulate_list(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, f);
+                            cnt = 0;
+                        }
+                        uint32_t bits = quad_test<FORCE_STAGE>(qx, px, py, pz, cull2);
+                        if (!tm.active) bits = 0u;
+                        const uint32_t qb = 4u * (rsl + j * tm.S);
+                        while (bits) {
+                            const uint32_t b = (uint32_t)__ffs(bits) - 1u;
+                            bits &= bits - 1u;
+                            const uint32_t q = qb + b;
+                            // The particle itself passes too; it contributes exactly zero. Padding
+                            // entries never pass; the check only keeps the read inside the piece.
+                            list[(cnt++) * 32u + lane] = q < len ? slot[q] : ti;
+                        }
                     }
                 }
             }
-            accumulate_list(list, cnt, lane, pi, vi, pos_b, vel_b, sc.h, f);
+            accumulate_list(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, f);
 #pragma unroll
             for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
             if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
