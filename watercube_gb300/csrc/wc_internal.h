@@ -102,7 +102,7 @@ constexpr int SPH_THREADS = 256;
 // Candidates a warp stages in shared memory per cell in the density pass (padding included).
 constexpr int STAGE_CAP = 320;
 // 32-bit words of neighbour bit strings per particle (density pass -> force pass).
-constexpr int MASK_WORDS = 32;
+constexpr int MASK_WORDS = 48;
 // Force kernel dense path: per-lane neighbour list capacity ([CAP][32] words per warp).
 constexpr int FORCE_LIST_CAP = 16;
 
