@@ -3,16 +3,18 @@ on), printing one JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload dam1m|dam16k]
 
-value      particle-steps/s of K graph-launched steps, inputs resident in HBM, device time from
-           CUDA events around each step; L2 is flushed (a read of twice its size) before every
-           timed step, outside the timed span.
-e2e        the same metric through the C ABI with host buffers: each step uploads the particle
-           state from pinned host memory, runs update(), and reads the state back.
-roofline   the dominant kernel's algorithmic bytes per launch / its CUDA-event time, against the
-           measured HBM copy bandwidth; `traffic` is its DRAM bytes per launch from ncu
-           (profiles/ncu_traffic.json).
+value      particle-steps/s of K graph-launched steps (the timed window: steps W+1 .. W+K of the
+           workload from its initial state), inputs resident in HBM, device time from CUDA events
+           around each step; L2 is flushed (a read of twice its size) before every timed step,
+           outside the timed span.
+e2e        the same metric over the same window through the C ABI with host buffers: each step
+           uploads the particle state from pinned host memory, runs update(), and reads it back.
+roofline   the dominant kernel's algorithmic bytes per launch / its mean CUDA-event time over the
+           same window (separately launched kernels), against the measured HBM copy bandwidth;
+           `traffic` is its DRAM bytes per launch from ncu (profiles/ncu_traffic.json).
 cpu_baseline  the CPU transcription of the reference's stages (oracle, FP32) on this host's
-           cores, on a bounded sample of the same workload.
+           cores, on a bounded sample of the same window (a few steps from states spread over it).
+--advance N  runs N untimed steps before the warm-up, to time or profile a later window.
 --impl reference  times the reference's own shader code compiled for the host CPU
            (oracle/_ref, when built) or else the oracle's transcription, all threads.
 surface    surface extraction of the same state: colour field on 256^3 vertices and marching
@@ -164,32 +166,42 @@ def dist_setup(gpus: int):
     return rank, world, local, reduce_max, dist.barrier
 
 
-def cpu_baseline(p, state, dt, threads_all: int):
-    """The oracle's FP32 transcription on a bounded sample of the workload (about 10 s of CPU
-    work at 1M particles): 40 full steps on all threads, then 6 full steps on one thread."""
+def cpu_baseline(p, samples, dt, threads_all: int):
+    """The oracle's FP32 transcription on a bounded sample of the timed window (about 20 s of CPU
+    work at 1M particles): from each state in `samples` ((window step, particles) pairs spread
+    evenly over the window, taken from the GPU run), 8 full steps on all threads and 1 on one
+    thread. A step's cost grows as the fluid compresses, so the per-step times are averaged
+    over the states, as the GPU's are over the window."""
     from oracle.oracle import Oracle
 
     o = Oracle()
-    n = state.shape[0]
-    s = state.copy()
-    o.step(p, s, dt, 1, threads=threads_all)  # warm-up (page-in, thread pool)
-    k_all, k_one = 40, 6
-    t = time.perf_counter()
-    o.step(p, s, dt, k_all, threads=threads_all)
-    t_all = (time.perf_counter() - t) / k_all
-    t = time.perf_counter()
-    o.step(p, s, dt, k_one, threads=1)
-    t_one = (time.perf_counter() - t) / k_one
+    n = samples[0][1].shape[0]
+    o.step(p, samples[0][1].copy(), dt, 1, threads=threads_all)  # warm-up (page-in, thread pool)
+    k_all, k_one = 8, 1
+    t_all, t_one = [], []
+    for _, state in samples:
+        s = state.copy()
+        t = time.perf_counter()
+        o.step(p, s, dt, k_all, threads=threads_all)
+        t_all.append((time.perf_counter() - t) / k_all)
+        s = state.copy()
+        t = time.perf_counter()
+        o.step(p, s, dt, k_one, threads=1)
+        t_one.append((time.perf_counter() - t) / k_one)
+    m_all, m_one = float(np.mean(t_all)), float(np.mean(t_one))
+    at = ", ".join(str(k) for k, _ in samples)
     return {
-        "value": n / t_all,
+        "value": n / m_all,
         "unit": UNIT,
         "cores": threads_all,
         "kind": "port",
-        "sample": f"{k_all} full steps on all threads, then {k_one} on one thread, of the {n}-particle workload "
-                  "from its initial state (the oracle's FP32 transcription of the reference's shader stages)",
-        "value_1thread": n / t_one,
-        "ms_per_step": t_all * 1e3,
-        "ms_per_step_1thread": t_one * 1e3,
+        "sample": f"{k_all} full steps on all threads and {k_one} on one thread from each of {len(samples)} states of "
+                  f"the timed window (window steps {at}; states from the GPU run), per-step times averaged over the "
+                  f"states; the {n}-particle workload, the oracle's FP32 transcription of the reference's shader stages",
+        "value_1thread": n / m_one,
+        "ms_per_step": m_all * 1e3,
+        "ms_per_step_1thread": m_one * 1e3,
+        "ms_per_step_by_state": [round(x * 1e3, 2) for x in t_all],
     }
 
 
@@ -252,7 +264,9 @@ def run_reference(args):
         "data": "synthetic",
         "config": {"workload": desc, "particles": n, "grid_res": int(p.grid_res), "dt": dt},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": f"{args.steps} full steps of the {n}-particle workload: {what}"},
+                         "sample": f"{args.steps} full steps of the {n}-particle workload after {args.warmup} warm-up "
+                                   "steps from its initial state (its cheapest part: a step's cost grows as the fluid "
+                                   f"compresses): {what}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -367,6 +381,8 @@ def run_ours(args):
     cells = int(p.grid_res) ** 3
     f = Fluid.create("bench", p)
     f.setup(st)
+    if args.advance:
+        f.step(dt, args.advance)
     # warm-up: graph capture, clocks up
     f.step(dt, max(args.warmup, 3))
     f.synchronize()
@@ -380,8 +396,26 @@ def run_ours(args):
     clock_summary = clocks.summary()
     value = world * n * args.steps / (total_ms * 1e-3)
 
-    # per-kernel CUDA-event times (separate launches of the same steps, L2 flushed before each)
-    _, kern = f.time_steps(dt, args.steps, flush_l2=True, kernel_times=True)
+    def restart():
+        """Back to the timed window's first state: the initial particles and the warm-up steps
+        (steps are deterministic, so the window repeats bit for bit)."""
+        f.set_particles(st)
+        f.step(dt, args.advance + max(args.warmup, 3))
+        f.synchronize()
+
+    # Per-kernel CUDA-event times over the same window (separately launched steps, L2 flushed
+    # before each), in four parts; each part's first state is kept for the CPU sample.
+    restart()
+    samples, kern_parts, done = [], [], 0
+    for i in range(4):
+        k = args.steps * (i + 1) // 4 - done
+        if k == 0:
+            continue
+        samples.append((done, f.particles()))
+        _, kp = f.time_steps(dt, k, flush_l2=True, kernel_times=True, graph_steps=False)
+        kern_parts.append(kp)
+        done += k
+    kern = np.concatenate(kern_parts)
     names = Fluid.kernel_names()
     kmean = {k: float(np.mean(kern[:, i])) for i, k in enumerate(names)}
     dom = max(kmean, key=kmean.get)
@@ -399,7 +433,7 @@ def run_ours(args):
     aout = hout.particles(n)
     ain[:] = f.particles()
     lib = _abi.lib()
-    e2e_steps = max(5, min(args.steps, 50))
+    e2e_steps = args.steps  # the same window as the device-timed steps
 
     def e2e_step(src, dst):
         _abi.check(lib.wc_fluid_set_particles(f._handle, _abi.WC_BUFFER_STATE, src.ctypes.data, n))
@@ -409,6 +443,8 @@ def run_ours(args):
     for _ in range(2):
         e2e_step(ain, aout)
         ain, aout = aout, ain
+    restart()
+    ain[:] = f.particles()
     barrier()
     t = time.perf_counter()
     for _ in range(e2e_steps):
@@ -437,6 +473,8 @@ def run_ours(args):
             "cells": cells,
             "dt": dt,
             "l2": "flushed before every timed step (read of 2x L2), outside the timed span",
+            "window": f"steps {args.advance + max(args.warmup, 3) + 1} .. {args.advance + max(args.warmup, 3) + args.steps} "
+                      "from the initial state",
             "parallelism": f"{world} independent replicas" if world > 1 else "1 GPU",
         },
         "roofline": {
@@ -449,6 +487,7 @@ def run_ours(args):
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             "algorithmic_bytes_per_launch": algo,
             "traffic": ncu_traffic(dom, args.workload),
+            "traffic_source": "ncu, launch of step 1,000 (profiles/ncu_traffic.json)",
             "step": {"algorithmic_bytes_per_particle": step_algo_bytes(n, cells), "achieved": step_gbs,
                      "frac": step_gbs / peak},
         },
@@ -460,7 +499,7 @@ def run_ours(args):
         "clocks": clock_summary,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(p, st, dt, os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(p, samples, dt, os.cpu_count() or 1)
     if rank == 0 and world == 1 and not args.no_rollout and args.workload == "dam1m":
         line["rollout"] = run_rollouts(p, st, dt, args.rollout_steps)
         line["surface"] = run_surface(p, st)
@@ -531,6 +570,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-rollout", action="store_true")
     ap.add_argument("--rollout-steps", type=int, default=8)
+    ap.add_argument("--advance", type=int, default=0, help="untimed steps before the warm-up (single scenes)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -252,7 +252,8 @@ WC_API const char* wc_step_kernel_name(uint32_t index);
  * Run nsteps steps of dt, each preceded (outside its timed span) by an L2 flush when flush_l2 is
  * non-zero. step_ms[s] receives the device time of step s (graph launch, CUDA events).
  * kernel_ms, when not NULL, receives nsteps * wc_step_kernel_count() per-kernel times from a
- * second, separately launched run of the same steps with an event between kernels.
+ * further nsteps separately launched steps with an event between kernels (after the graph
+ * steps when step_ms is given; alone when step_ms is NULL). At least one of the two is given.
  */
 WC_API wc_status wc_fluid_time_steps(wc_fluid* f, float dt, uint32_t nsteps, int flush_l2, float* step_ms,
                                      float* kernel_ms);

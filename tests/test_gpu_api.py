@@ -125,3 +125,6 @@ def test_timing_entry_point(gpu):
         assert Fluid.kernel_names() == ["bin_count", "scan_cells", "scatter_cells", "rank_gather", "density",
                                         "force_integrate"]
         assert f.step_count == 8
+        none, kern2 = f.time_steps(1e-3, 3, kernel_times=True, graph_steps=False)
+        assert none is None and kern2.shape == (3, 6) and (kern2 > 0).all()
+        assert f.step_count == 11

@@ -526,7 +526,7 @@ WC_API wc_status wc_fluid_time_steps(wc_fluid* f, float dt, uint32_t nsteps, int
     clear_error();
     WC_NVTX("wc_fluid_time_steps");
     WC_TRY(require(f, true));
-    if (!step_ms && nsteps) return fail(WC_ERR_INVALID_ARG, "null step_ms");
+    if (!step_ms && !kernel_ms && nsteps) return fail(WC_ERR_INVALID_ARG, "null step_ms and kernel_ms");
     if (flush_l2 && !f->flush_buf) {
         int l2 = 0;
         cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, f->device);
@@ -540,17 +540,19 @@ WC_API wc_status wc_fluid_time_steps(wc_fluid* f, float dt, uint32_t nsteps, int
     std::vector<cudaEvent_t> ev(2 * (size_t)nsteps + 7, nullptr);
     for (auto& e : ev) WC_CUDA_TRY(cudaEventCreate(&e));
     wc_status st = WC_OK;
-    for (uint32_t s = 0; s < nsteps && st == WC_OK; ++s) {
-        if (flush_l2) launch_l2_flush(f->flush_buf, f->flush_n4, f->flush_sink, f->stream);
-        cudaEventRecord(ev[2 * s], f->stream);
-        st = launch_step(f, f->in);
-        cudaEventRecord(ev[2 * s + 1], f->stream);
-    }
-    if (st == WC_OK) st = read_device_errors(f);
-    for (uint32_t s = 0; s < nsteps && st == WC_OK; ++s) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev[2 * s], ev[2 * s + 1]);
-        step_ms[s] = ms;
+    if (step_ms) {
+        for (uint32_t s = 0; s < nsteps && st == WC_OK; ++s) {
+            if (flush_l2) launch_l2_flush(f->flush_buf, f->flush_n4, f->flush_sink, f->stream);
+            cudaEventRecord(ev[2 * s], f->stream);
+            st = launch_step(f, f->in);
+            cudaEventRecord(ev[2 * s + 1], f->stream);
+        }
+        if (st == WC_OK) st = read_device_errors(f);
+        for (uint32_t s = 0; s < nsteps && st == WC_OK; ++s) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[2 * s], ev[2 * s + 1]);
+            step_ms[s] = ms;
+        }
     }
     if (st == WC_OK && kernel_ms) {
         cudaEvent_t* ke = ev.data() + 2 * (size_t)nsteps;  // 7 events: around and between kernels

@@ -253,15 +253,19 @@ class Fluid:
         check(lib().wc_fluid_get_device_buffers(self._require(), C.byref(b)))
         return b
 
-    def time_steps(self, dt: float, nsteps: int, flush_l2: bool = True, kernel_times: bool = False):
+    def time_steps(self, dt: float, nsteps: int, flush_l2: bool = True, kernel_times: bool = False,
+                   graph_steps: bool = True):
         """Device times (ms) of nsteps graph-launched steps; optionally per-kernel times of a
-        second run of nsteps individually launched steps. Advances the simulation."""
-        step_ms = np.zeros(nsteps, dtype=np.float32)
+        further nsteps individually launched steps (graph_steps=False: those alone, and the
+        step times returned are None). Advances the simulation."""
+        if not graph_steps and not kernel_times:
+            raise A.WatercubeError(A.WC_ERR_INVALID_ARG, "nothing to time")
+        step_ms = np.zeros(nsteps, dtype=np.float32) if graph_steps else None
         nk = lib().wc_step_kernel_count()
         kern = np.zeros((nsteps, nk), dtype=np.float32) if kernel_times else None
         check(
             lib().wc_fluid_time_steps(
-                self._require(), float(dt), nsteps, int(flush_l2), A._ptr(step_ms),
+                self._require(), float(dt), nsteps, int(flush_l2), A._ptr(step_ms) if step_ms is not None else None,
                 A._ptr(kern) if kern is not None else None,
             ),
             "wc_fluid_time_steps",
