@@ -505,7 +505,7 @@ WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, w
     if (st == WC_OK) st = dalloc(&d.counts, cells);
     if (st == WC_OK) st = dalloc(&d.start, cells + 1);
     if (st == WC_OK) st = dalloc(&d.cell_list, cells);
-    if (st == WC_OK) st = dalloc(&d.num_nonempty, 1);
+    if (st == WC_OK) st = dalloc(&d.num_nonempty, 3);
     if (st == WC_OK) st = dalloc(&d.scan_desc, tiles_cap);
     if (st == WC_OK) st = dalloc(&d.scan_tile_counter, 1);
     if (st == WC_OK) st = dalloc(&d.err, 1);
@@ -520,7 +520,7 @@ WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, w
         st = fail(WC_ERR_CUDA, "table upload failed");
     if (st == WC_OK) {
         cudaMemsetAsync(d.err, 0, sizeof(uint32_t), b->stream);
-        cudaMemsetAsync(d.num_nonempty, 0, sizeof(uint32_t), b->stream);
+        cudaMemsetAsync(d.num_nonempty, 0, 3 * sizeof(uint32_t), b->stream);
         cudaMemsetAsync(d.start, 0, sizeof(uint32_t) * (cells + 1), b->stream);
         if (n) cudaMemsetAsync(d.hits, 0, sizeof(uint32_t) * MASK_WORDS * (size_t)n, b->stream);
         b->ld = compute_launch_dims(b->device);

@@ -96,14 +96,14 @@ wc_status allocate(wc_fluid* f) {
     WC_TRY(dalloc(&d.counts, d.num_cells));
     WC_TRY(dalloc(&d.start, (size_t)d.num_cells + 1));
     WC_TRY(dalloc(&d.cell_list, d.num_cells));
-    WC_TRY(dalloc(&d.num_nonempty, 1));
+    WC_TRY(dalloc(&d.num_nonempty, 3));
     WC_TRY(dalloc(&d.scan_desc, d.num_tiles));
     WC_TRY(dalloc(&d.scan_tile_counter, 1));
     WC_TRY(dalloc(&d.err, 1));
     WC_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&f->h_err), sizeof(uint32_t)));
     WC_CUDA_TRY(cudaMemsetAsync(d.counts, 0, sizeof(uint32_t) * d.num_cells, f->stream));
     WC_CUDA_TRY(cudaMemsetAsync(d.start, 0, sizeof(uint32_t) * ((size_t)d.num_cells + 1), f->stream));
-    WC_CUDA_TRY(cudaMemsetAsync(d.num_nonempty, 0, sizeof(uint32_t), f->stream));
+    WC_CUDA_TRY(cudaMemsetAsync(d.num_nonempty, 0, 3 * sizeof(uint32_t), f->stream));
     WC_CUDA_TRY(cudaMemsetAsync(d.err, 0, sizeof(uint32_t), f->stream));
     if (n) {
         WC_CUDA_TRY(cudaMemsetAsync(d.pos_a, 0, sizeof(float4) * n, f->stream));

@@ -118,6 +118,8 @@ struct DevBuffers {
     uint32_t *counts;     // [C] histogram (zero between steps)
     uint32_t *start;      // [C+1] exclusive prefix + total
     uint32_t *cell_list;  // [C] non-empty cells, ascending
+    // [0]: non-empty cells (written by the scan); [1], [2]: the density and force passes' cell
+    // counters (dynamic scheduling; zeroed before each launch)
     uint32_t *num_nonempty;
     unsigned long long* scan_desc;  // [num_tiles]
     uint32_t* scan_tile_counter;
@@ -173,7 +175,7 @@ struct ForceKernelArgs {
     uint32_t* ids_a;
     const uint32_t* start;
     const uint32_t* cell_list;
-    const uint32_t* num_nonempty;
+    uint32_t* num_nonempty;
     const uint32_t* hits;
     float4* accel;
     uint32_t* err;

@@ -6,8 +6,8 @@
 //                                        and mouse forces), fused with symplectic Euler and the
 //                                        box-wall collision
 //
-// Work decomposition (both kernels): a warp owns one non-empty cell at a time (grid-stride over
-// the cell list the scan produced). The 27 neighbour cells of a cell form 9 rows of 3 cells
+// Work decomposition (both kernels): a warp owns one non-empty cell at a time, taking the next
+// index into the cell list the scan produced from a counter (dynamic scheduling). The 27 neighbour cells of a cell form 9 rows of 3 cells
 // that are contiguous in key order, hence 9 contiguous ranges of the sorted particle buffer;
 // lanes 0..8 look them up once per cell and a 9-lane scan numbers the concatenated candidate
 // list 0 .. L-1. The warp's 32 lanes are split into nt targets (the cell's particles, up to 32
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
                                                                  float* p_out,    // aliases vel[].w
                                                                  const uint32_t* __restrict__ start,
                                                                  const uint32_t* __restrict__ cell_list,
-                                                                 const uint32_t* __restrict__ num_nonempty,
+                                                                 uint32_t* __restrict__ num_nonempty,  // [0] cells, [1]/[2] counters
                                                                  uint32_t* __restrict__ ncount,
                                                                  uint32_t* __restrict__ hits,
                                                                  uint32_t* __restrict__ err) {
@@ -425,10 +425,13 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
     float* sx = s_stage[threadIdx.x >> 5][0];
     float* sy = s_stage[threadIdx.x >> 5][1];
     float* sz = s_stage[threadIdx.x >> 5][2];
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t M = min(*num_nonempty, num_cells);
-    for (uint32_t m = warp; m < M; m += nwarps) {
+    const uint32_t M = min(num_nonempty[0], num_cells);
+    // Dynamic scheduling: each warp takes the next cell from a counter (the next index is
+    // fetched while the current cell runs), so dense cells do not pile up on a few warps.
+    uint32_t* const counter = num_nonempty + 1;
+    uint32_t m_next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
+    for (uint32_t m = __shfl_sync(FULL, m_next, 0); m < M; m = __shfl_sync(FULL, m_next, 0)) {
+        if (lane == 0) m_next = atomicAdd(counter, 1u);
         const uint32_t cg = __ldg(cell_list + m);
         SceneConsts sc;
         uint32_t coff = 0;
@@ -690,7 +693,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                                                                uint32_t* __restrict__ ids_a,
                                                                const uint32_t* __restrict__ start,
                                                                const uint32_t* __restrict__ cell_list,
-                                                               const uint32_t* __restrict__ num_nonempty,
+                                                               uint32_t* __restrict__ num_nonempty,  // [0] cells, [1]/[2] counters
                                                                const uint32_t* __restrict__ hits,
                                                                float4* __restrict__ accel,
                                                                uint32_t* __restrict__ err) {
@@ -706,10 +709,13 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
     uint32_t* slot = s_work[threadIdx.x >> 5];
     uint32_t* list = slot + STAGE_CAP;
     float* fx = reinterpret_cast<float*>(list + FORCE_LIST_CAP * 32);
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t M = min(*num_nonempty, num_cells);
-    for (uint32_t m = warp; m < M; m += nwarps) {
+    const uint32_t M = min(num_nonempty[0], num_cells);
+    // Dynamic scheduling: each warp takes the next cell from a counter (the next index is
+    // fetched while the current cell runs), so dense cells do not pile up on a few warps.
+    uint32_t* const counter = num_nonempty + 2;
+    uint32_t m_next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
+    for (uint32_t m = __shfl_sync(FULL, m_next, 0); m < M; m = __shfl_sync(FULL, m_next, 0)) {
+        if (lane == 0) m_next = atomicAdd(counter, 1u);
         const uint32_t cg = __ldg(cell_list + m);
         SceneConsts sc;
         uint32_t coff = 0;
@@ -977,6 +983,7 @@ LaunchDims compute_launch_dims(int device) {
 }
 
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s) {
+    cudaMemsetAsync(d.num_nonempty + 1, 0, sizeof(uint32_t), s);  // the pass's cell counter
     density_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
         sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
         reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty,
@@ -985,12 +992,14 @@ void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims
 
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s) {
+    cudaMemsetAsync(d.num_nonempty + 2, 0, sizeof(uint32_t), s);
     force_kernel<false><<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, BatchTables{}, in, d.n, d.num_cells, d.pos_b,
                                                               d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
                                                               d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
 }
 
 void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
+    cudaMemsetAsync(d.num_nonempty + 1, 0, sizeof(uint32_t), s);
     density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
         SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
         reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
@@ -998,6 +1007,7 @@ void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const La
 
 void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
                           cudaStream_t s) {
+    cudaMemsetAsync(d.num_nonempty + 2, 0, sizeof(uint32_t), s);
     force_kernel<true><<<ld.grid_force, SPH_THREADS, 0, s>>>(SceneConsts{}, bt, in, d.n, d.num_cells, d.pos_b,
                                                              d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
                                                              d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
