@@ -22,10 +22,12 @@
 // passed as a bit string. The force pass decodes those bits once per cell into one neighbour
 // list per target (shared memory, prefix sums over the target's slices), and the target's
 // slices then split its list evenly, gathering four neighbours per round, instead of testing
-// all candidates again. Cells whose candidate list does not fit the stage, cells of more than
-// 32 particles and bit strings longer than the per-particle slot take the direct path: the
-// density pass reads candidates from global memory and the force pass culls into per-lane
-// shared-memory lists.
+// all candidates again. Compressed states outgrow that form: a candidate list longer than the
+// stage streams through it in pieces (dense path), and a cell of more than 32 particles is
+// taken 32 targets at a time. Their bit strings are kept whenever a chunk's words fit the
+// per-particle slot (bits_fit), in pieces whole words long, and the force pass replays them
+// piece by piece through slot tables into per-lane lists; where they are not kept, the force
+// pass culls the candidates itself with the same packed test through a small stage.
 //
 // Neighbour test: |r| < h is evaluated exactly as sqrtf(fma(dz,dz,fma(dy,dy,dx*dx))) < h would
 // be, as d2 <= cull with cull = the largest float whose sqrtf is below h, so the neighbour
