@@ -39,6 +39,27 @@ def case(name: str, extra_flags: int = 0):
         p.flags |= extra_flags
         p = finalize(p)
         return p, generate_reference_lattice(p, 0)
+    if name == "compressed16k":
+        # A dense block (spacing 0.3 h: ~37 particles per cell, ~1,000 candidates) and a denser
+        # one (0.2 h: ~125 per cell, ~3,400 candidates): candidate lists longer than the stage,
+        # cells of more than 32 particles, bit strings kept in pieces and bit strings that do
+        # not fit the slot -- every dense path of the two neighbour passes, beside the block
+        # edges' ordinary cells.
+        p = dam_break_params(16384)
+        p.flags |= extra_flags
+        p = finalize(p)
+        st = generate_dam_break(p, 0)
+        rng = np.random.default_rng(7)
+        h = float(p.kernel_radius)
+
+        def block(count, spacing, origin):
+            k = int(np.ceil(count ** (1.0 / 3.0)))
+            g = np.stack(np.meshgrid(*[np.arange(k)] * 3, indexing="ij"), -1).reshape(-1, 3)[:count]
+            return origin + g * spacing + rng.uniform(-0.01 * h, 0.01 * h, (count, 3))
+
+        st["position"] = np.concatenate([block(12000, 0.3 * h, 0.05), block(4384, 0.2 * h, 0.6)]).astype(np.float32)
+        st["velocity"] = rng.normal(0.0, 0.2, (16384, 3)).astype(np.float32)
+        return p, st
     if name == "dam16k_refphysics":
         p = reference_physics(dam_break_params(16384))
         p.stiffness = 100.0

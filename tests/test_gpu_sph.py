@@ -24,6 +24,7 @@ CASES = [
     ("dam16k_refphysics", 10, 2e-4),
     ("dam16k_walls", 30, 1e-3),
     ("dam1m", 4, 2.5e-4),
+    ("compressed16k", 3, 1e-4),
 ]
 
 
