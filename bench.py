@@ -76,13 +76,57 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str, workload: str):
+def ncu_capture(workload: str, window_mid: float):
+    """The ncu capture of `workload` (profiles/ncu_traffic.json) whose step is nearest the middle
+    of the timed window: per kernel its DRAM bytes and warp-instructions per launch. A step's
+    cost changes as the fluid compresses, so the capture must match the window."""
     p = REPO / "profiles" / "ncu_traffic.json"
     if not p.is_file():
         return None
-    d = json.loads(p.read_text())
-    e = d.get(workload, {}).get(kernel)
-    return None if e is None else float(e)
+    caps = [c for c in json.loads(p.read_text()).get("captures", []) if c.get("workload") == workload]
+    if not caps:
+        return None
+    return min(caps, key=lambda c: abs(float(c["step"]) - window_mid))
+
+
+def sm_count(device: int) -> int:
+    try:
+        import torch
+
+        return int(torch.cuda.get_device_properties(device).multi_processor_count)
+    except Exception:
+        return 152  # GB300
+
+
+def issue_bound(cap: dict, kernel: str, ms: float, sms: int, sm_mhz: float, n: int):
+    """The instruction-issue roofline of `kernel`: its warp-instructions per launch (ncu,
+    smsp__inst_executed.sum of the matching capture) over its mean CUDA-event time, against the
+    SMs' issue rate (4 schedulers x one warp-instruction per cycle each, at the median SM clock
+    sampled during the timed region)."""
+    inst = cap.get("warp_instructions", {}).get(kernel)
+    if inst is None:
+        return None
+    achieved = float(inst) / (ms * 1e-3) / 1e9
+    peak = sms * 4 * sm_mhz * 1e6 / 1e9
+    return {"bound": "issue", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "G warp-instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_particle": float(inst) / n,
+            "peak_source": f"{sms} SMs x 4 schedulers x {sm_mhz:.0f} MHz (median sampled SM clock)",
+            "instructions_source": f"ncu smsp__inst_executed.sum, launch of step {cap['step']}"}
+
+
+def workload_config(workload: str, n: int, grid_res: int, dt: float, first: int, last: int, world: int) -> dict:
+    """The `config` object of both arms (identical for the same workload, window and N)."""
+    return {
+        "workload": WORKLOADS[workload][2],
+        "particles_per_gpu": n,
+        "grid_res": grid_res,
+        "cells": grid_res ** 3,
+        "dt": dt,
+        "window": f"steps {first} .. {last} from the initial state",
+        "l2": "GPU arm: flushed before every timed step (read of 2x L2), outside the timed span; "
+              "CPU arm: not applicable",
+        "parallelism": f"{world} independent replicas" if world > 1 else "1 GPU",
+    }
 
 
 class Clocks:
@@ -206,16 +250,19 @@ def cpu_baseline(p, samples, dt, threads_all: int):
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU implementation of the path on this host."""
+    """--impl reference: the reference's CPU implementation of the path on this host. Only the
+    oracle libraries are loaded (parameters and the initial lattice come from the oracle too):
+    nothing of the solver runs in this arm."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return 0
     from oracle.oracle import Oracle, RefLib, build_ref, ref_available
-    from watercube_gb300.fluid import dam_break_params, finalize, generate_dam_break
 
     n, dt, desc = WORKLOADS[args.workload]
-    p = finalize(dam_break_params(n))
-    st = generate_dam_break(p, 0)
+    o = Oracle()
+    p = o.dam_break_params(n)
+    st = o.generate_dam_break(p, 0)
     threads = os.cpu_count() or 1
     kind = "port"
     try:
@@ -225,20 +272,18 @@ def run_reference(args):
             kind = "reference"
     except Exception:
         kind = "port"
+    state = st.copy()
     if kind == "reference":
         ref = RefLib()
-        state = st.copy()
 
         def one_step():
             ref.step(p, state, dt, 1, threads=threads)
     else:
-        o = Oracle()
-        state = st.copy()
-
         def one_step():
             o.step(p, state, dt, 1, threads=threads)
 
-    for _ in range(args.warmup):
+    warm = args.advance + max(args.warmup, 3)
+    for _ in range(warm):
         one_step()
     t = time.perf_counter()
     for _ in range(args.steps):
@@ -262,11 +307,10 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": desc, "particles": n, "grid_res": int(p.grid_res), "dt": dt},
+        "config": workload_config(args.workload, n, int(p.grid_res), dt, warm + 1, warm + args.steps, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": f"{args.steps} full steps of the {n}-particle workload after {args.warmup} warm-up "
-                                   "steps from its initial state (its cheapest part: a step's cost grows as the fluid "
-                                   f"compresses): {what}"},
+                         "sample": f"{args.steps} full steps of the {n}-particle workload after {warm} untimed steps "
+                                   f"from its initial state (the same window as the GPU arm): {what}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -424,6 +468,11 @@ def run_ours(args):
     achieved = algo / (kmean[dom] * 1e-3) / 1e9
     step_mean_ms = total_ms / args.steps
     step_gbs = step_algo_bytes(n, cells) * n / (step_mean_ms * 1e-3) / 1e9
+    first = args.advance + max(args.warmup, 3) + 1
+    last = first + args.steps - 1
+    cap = ncu_capture(args.workload, 0.5 * (first + last))
+    sm_mhz = (clock_summary or {}).get("sm_mhz") or 2070.0
+    issue = issue_bound(cap, dom, kmean[dom], sm_count(local), sm_mhz, n) if cap else None
 
     # end to end through the C ABI with host buffers
     nbytes = n * 32
@@ -466,17 +515,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {
-            "workload": desc,
-            "particles_per_gpu": n,
-            "grid_res": int(p.grid_res),
-            "cells": cells,
-            "dt": dt,
-            "l2": "flushed before every timed step (read of 2x L2), outside the timed span",
-            "window": f"steps {args.advance + max(args.warmup, 3) + 1} .. {args.advance + max(args.warmup, 3) + args.steps} "
-                      "from the initial state",
-            "parallelism": f"{world} independent replicas" if world > 1 else "1 GPU",
-        },
+        "config": workload_config(args.workload, n, int(p.grid_res), dt, first, last, world),
         "roofline": {
             "bound": "hbm",
             "kernel": dom,
@@ -486,10 +525,12 @@ def run_ours(args):
             "frac": achieved / peak,
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
             "algorithmic_bytes_per_launch": algo,
-            "traffic": ncu_traffic(dom, args.workload),
-            "traffic_source": "ncu, launch of step 1,000 (profiles/ncu_traffic.json)",
+            "traffic": float(cap["dram_bytes"][dom]) if cap and dom in cap.get("dram_bytes", {}) else None,
+            "traffic_source": (f"ncu, launch of step {cap['step']} (the capture nearest the window's middle, "
+                               "profiles/ncu_traffic.json)") if cap else None,
             "step": {"algorithmic_bytes_per_particle": step_algo_bytes(n, cells), "achieved": step_gbs,
                      "frac": step_gbs / peak},
+            "issue": issue,
         },
         "kernels_ms": kmean,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,

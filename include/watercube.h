@@ -512,7 +512,7 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
  * cell table, positions gathered into sorted order) as one call that allocates no memory, for
  * callers that cannot allocate when they sort: a frame loop where cudaMalloc would synchronise
  * the GPU, or a host application that fixes its device memory budget up front. Its scratch is
- * one fixed device array (about 8 MB) held by every GPU that loads the library, so it accepts
+ * one fixed device array (about 4 MB) held by every GPU that loads the library, so it accepts
  * at most WC_NOALLOC_MAX_PARTICLES particles and WC_NOALLOC_MAX_CELLS cells and rejects more
  * with WC_ERR_INVALID_ARG. All buffers are device memory the caller owns:
  *   d_positions        float4[n] (x, y, z, anything)        input
@@ -523,10 +523,21 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
  * Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and not waited for. The
  * first call on a device looks up the array's address and should come before any stream capture.
  * Calls share the array: calls that overlap on the GPU race, so order them on one stream.
+ * Device-side errors are not returned by this call (it does not wait); see
+ * wc_sort_cells_noalloc_status.
  */
 WC_API wc_status wc_sort_cells_noalloc(const void* d_positions, uint32_t n, uint32_t grid_res, float bin_size,
                                        uint32_t* d_keys, uint32_t* d_permutation, uint32_t* d_cell_start,
                                        void* d_sorted_positions, void* stream);
+
+/*
+ * No counterpart in the reference. Waits for `stream` and reports the device-side errors of the
+ * last wc_sort_cells_noalloc call on the current device, without allocating: WC_ERR_TIMEOUT when
+ * a scan tile gave up waiting (that call's cell table and permutation are invalid),
+ * WC_ERR_NUMERIC for a non-finite position (binned to cell 0) or a cell of more than 65,536
+ * particles (its members are placed in arrival order, not input order), else WC_OK.
+ */
+WC_API wc_status wc_sort_cells_noalloc_status(void* stream);
 
 /* Make `device` current for handles created afterwards on this thread (one process per GPU). */
 /* Test hook, not for production use: with on != 0 the cell scan's look-back polls a descriptor

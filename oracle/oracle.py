@@ -72,6 +72,8 @@ class Oracle:
             ("wco_update_f64", C.c_int, [pp, P, P, u32, P, P, C.c_double, C.c_int]),
             ("wco_step_f32", C.c_int, [pp, P, u32, C.c_float, u32, P, C.c_int]),
             ("wco_step_f64", C.c_int, [pp, P, u32, C.c_double, u32, P, C.c_int]),
+            ("wco_params_dam_break", C.c_int, [pp, u32]),
+            ("wco_params_finalize", C.c_int, [pp]),
             ("wco_generate_dam_break", C.c_int, [pp, C.c_uint64, P, u32]),
             ("wco_generate_reference_lattice", C.c_int, [pp, C.c_uint64, P, u32]),
             ("wco_diagnostics_f32", C.c_int, [pp, P, u32, C.POINTER(Diagnostics)]),
@@ -122,6 +124,14 @@ class Oracle:
         """In place on `state` (and `ids`)."""
         fn = self.lib.wco_step_f64 if state.dtype == PARTICLE64_DTYPE else self.lib.wco_step_f32
         assert fn(C.byref(p), _p(state), state.shape[0], float(dt), nsteps, _p(ids), threads) == 0
+
+    def dam_break_params(self, n: int) -> Params:
+        """The dam-break preset at n particles, finalized, computed by the oracle library alone
+        (no solver library is loaded)."""
+        p = Params()
+        assert self.lib.wco_params_dam_break(C.byref(p), n) == 0
+        assert self.lib.wco_params_finalize(C.byref(p)) == 0
+        return p
 
     def generate_dam_break(self, p, seed=0):
         out = np.zeros(p.num_particles, PARTICLE_DTYPE)

@@ -1,7 +1,7 @@
 """Build the parity reference: WaterCube's own GLSL compute shaders compiled as C++.
 
 TEST INFRASTRUCTURE ONLY. This recipe reads the reference's shader sources where they lie
-(default /root/reference, or $WC_REFERENCE_ROOT), removes the three GLSL-only constructs that
+($WC_REFERENCE_ROOT, else a checkout named `reference` beside the repository), removes the three GLSL-only constructs that
 C++ cannot parse, and compiles each shader unchanged otherwise against oracle/ref/glsl_compat.h:
 
   * the `#version` line;
@@ -54,7 +54,10 @@ _UNIFORM = re.compile(r"^\s*uniform\s+(\w+)\s+(\w+)\s*;", re.M)
 
 
 def reference_root() -> Path | None:
-    root = Path(os.environ.get("WC_REFERENCE_ROOT", "/root/reference"))
+    """$WC_REFERENCE_ROOT when set, else a WaterCube checkout named `reference` beside this
+    repository's directory; None when neither holds the shaders."""
+    env = os.environ.get("WC_REFERENCE_ROOT")
+    root = Path(env) if env else Path(__file__).resolve().parents[3] / "reference"
     return root if (root / "assets" / "sort" / "count.comp").is_file() else None
 
 

@@ -534,6 +534,56 @@ int wco_generate_reference_lattice(const wc_params* p, uint64_t seed, wc_particl
     return 0;
 }
 
+// The dam-break workload's constants: h = 0.0457 (16384/n)^(1/3), lattice spacing h/2,
+// m = 1000 (h/2)^3, rho0 = 1000, k = 3, mu = 3.5, g = (0, -9.81, 0), linear EOS, restitution 0.5,
+// none of the reference-only extras.
+int wco_params_dam_break(wc_params* p, uint32_t n) {
+    if (!p) return -1;
+    std::memset(p, 0, sizeof *p);
+    const double h = 0.0457 * std::cbrt(16384.0 / (double)(n ? n : 1));
+    const double s = 0.5 * h;
+    p->num_particles = n;
+    p->size = 1.0f;
+    p->kernel_radius = (float)h;
+    p->particle_radius = (float)(h / 4.0);
+    p->particle_mass = (float)(1000.0 * s * s * s);
+    p->rest_density = 1000.0f;
+    p->stiffness = 3.0f;
+    p->viscosity = 3.5f;
+    p->gravity[1] = -9.81f;
+    p->time_scale = 1.0f;
+    p->eos = WC_EOS_LINEAR;
+    p->max_speed = 50.0f;
+    p->wall_damping = 0.5f;
+    p->wall_border = 0.001f;
+    p->mouse_origin[1] = 2.0f;
+    p->mouse_dir[1] = 1.0f;
+    return 0;
+}
+
+// Fluid::setup's derived quantities (src/core/Fluid.cpp:207-216): h = 4 r_p and m = 8 r_p
+// when unset, the grid floor(size / h), bin = size / R, and the Poly6 / Spiky / viscosity
+// constants evaluated in double and rounded to float, as glm::pow on doubles then the float
+// uniform do.
+int wco_params_finalize(wc_params* p) {
+    if (!p || !(p->size > 0.0f)) return -1;
+    if (p->kernel_radius == 0.0f) p->kernel_radius = p->particle_radius * 4.0f;
+    if (p->particle_mass == 0.0f) p->particle_mass = p->particle_radius * 8.0f;
+    if (!(p->kernel_radius > 0.0f) || !(p->particle_mass > 0.0f)) return -1;
+    if (p->grid_res == 0) {
+        const float r = std::floor(p->size / p->kernel_radius);
+        p->grid_res = r < 1.0f ? 1u : (uint32_t)r;
+    }
+    if (p->grid_res > 1024) return -1;
+    if (p->bin_size == 0.0f) p->bin_size = p->size / (float)p->grid_res;
+    const double h = p->kernel_radius;
+    const double pi = 3.14159265358979323846;
+    if (p->poly6_const == 0.0f) p->poly6_const = (float)(315.0 / (64.0 * pi * std::pow(h, 9)));
+    if (p->spiky_const == 0.0f) p->spiky_const = (float)(-45.0 / (pi * std::pow(h, 6)));
+    if (p->visc_const == 0.0f) p->visc_const = (float)(45.0 / (pi * std::pow(h, 6)));
+    return 0;
+}
+
 int wco_diagnostics_f32(const wc_params* p, const wc_particle* s, uint32_t n, wco_diagnostics* out) {
     if (!p || !out) return -1;
     return diagnostics_impl<float>(p, reinterpret_cast<const Particle<float>*>(s), n, out);

@@ -72,6 +72,11 @@ int wco_step_f64(const wc_params* p, wco_particle64* state, uint32_t n, double d
 int wco_generate_dam_break(const wc_params* p, uint64_t seed, wc_particle* out, uint32_t n);
 int wco_generate_reference_lattice(const wc_params* p, uint64_t seed, wc_particle* out, uint32_t n);
 
+/* Parameters without the solver library: the dam-break preset and Fluid::setup's derivation
+   (src/core/Fluid.cpp:207-216); the same values as wc_params_dam_break / wc_params_finalize. */
+int wco_params_dam_break(wc_params* p, uint32_t n);
+int wco_params_finalize(wc_params* p);
+
 int wco_diagnostics_f32(const wc_params* p, const wc_particle* s, uint32_t n, wco_diagnostics* out);
 int wco_diagnostics_f64(const wc_params* p, const wco_particle64* s, uint32_t n, wco_diagnostics* out);
 

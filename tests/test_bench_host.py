@@ -36,3 +36,34 @@ def test_cpu_baseline_averages_sampled_states():
     assert out["kind"] == "port" and out["cores"] == 2 and out["value"] > 0 and out["value_1thread"] > 0
     assert len(out["ms_per_step_by_state"]) == 2 and "window steps 0, 10" in out["sample"]
     assert np.isclose(out["value"], 4096 / (np.mean(out["ms_per_step_by_state"]) * 1e-3), rtol=1e-2)
+
+
+def test_reference_arm_loads_no_solver_library():
+    """The reference arm takes its parameters and initial lattice from the oracle library: the
+    process never maps libwatercube.so, and its config equals the GPU arm's for the same window."""
+    code = (
+        "import argparse, json, sys; sys.path.insert(0, '.'); import bench\n"
+        "a = argparse.Namespace(workload='dam16k', steps=1, warmup=3, advance=0, gpus=1)\n"
+        "bench.run_reference(a)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'loaded': 'libwatercube' in maps}))\n"
+    )
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.strip().splitlines()]
+    assert lines[-1] == {"loaded": False}
+    sys.path.insert(0, str(REPO))
+    import bench
+
+    assert lines[0]["config"] == bench.workload_config("dam16k", 16384, lines[0]["config"]["grid_res"], 1e-3, 4, 4, 1)
+
+
+def test_oracle_params_equal_the_solver_params():
+    from oracle.oracle import Oracle
+    from watercube_gb300.fluid import dam_break_params, finalize
+
+    o = Oracle()
+    for n in (1, 4096, 16384, 1048576):
+        a = o.dam_break_params(n)
+        b = finalize(dam_break_params(n))
+        assert bytes(a) == bytes(b), n

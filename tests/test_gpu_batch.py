@@ -7,7 +7,9 @@ import numpy as np
 import pytest
 
 from helpers import fluid
+from oracle.oracle import to64
 from watercube_gb300 import _abi
+from watercube_gb300.fluid import finalize
 from watercube_gb300.batch import Batch, batch_specs, scene_params, scene_particles
 
 pytestmark = pytest.mark.gpu
@@ -82,3 +84,42 @@ def test_workload_sample_runs(gpu):
         assert (out["position"] >= 0.0).all() and (out["position"] <= 1.0).all()
         off = b.offsets()
         assert off[-1] == out.shape[0] == sum(s.num_particles for s in specs)
+
+
+def test_coarser_cells_keep_the_densities(gpu, oracle):
+    """The tuner's other cell edge, 1.25 h, regrids every scene: the 27-cell search still covers
+    every pair within h, so after one step each scene's densities (those of the step's density
+    pass, carried in the state) stay within 1e-5 of the FP64 oracle on the scene's own 1.0 h
+    grid, and the positions agree with the 1.0 h run to FP32 rounding (only the order of the
+    neighbour sums changes)."""
+    _, params, states = small_batch(4, seed=9)
+    dt = 1e-3
+    runs = {}
+    for factor in (1.0, 1.25):
+        with Batch(params, states) as b:
+            t = b.tuning()
+            t.cell_factor = factor
+            b.set_tuning(t)
+            assert b.tuning().cell_factor == factor
+            b.step(dt, 1)
+            runs[factor] = (b.particles(), b.ids(), b.offsets())
+    out, ids, off = runs[1.25]
+    base, base_ids, _ = runs[1.0]
+    for s, (p, st) in enumerate(zip(params, states)):
+        p = finalize(p)
+        lo, hi = int(off[s]), int(off[s + 1])
+        n = hi - lo
+        rho = np.empty(n)
+        rho[ids[lo:hi] - lo] = out["density"][lo:hi]
+        o_sorted, _, o_perm, counts, offsets = oracle.sort(p, st)
+        s64 = to64(o_sorted)
+        oracle.density(p, s64, counts, offsets)
+        rho64 = np.empty(n)
+        rho64[o_perm] = s64["density"]
+        rel = np.abs(rho - rho64) / np.abs(rho64)
+        assert rel.max() <= 1e-5, (s, rel.max())
+        pos = np.empty((n, 3))
+        pos[ids[lo:hi] - lo] = out["position"][lo:hi]
+        ref = np.empty((n, 3))
+        ref[base_ids[lo:hi] - lo] = base["position"][lo:hi]
+        assert np.abs(pos - ref).max() <= 1e-5 * float(p.kernel_radius), s

@@ -161,6 +161,28 @@ def test_nonfinite_state_is_bounded(gpu):
         assert e.value.status == _abi.WC_ERR_NUMERIC
 
 
+def test_overfull_cell_sort_is_bounded(gpu):
+    """A million particles in one cell: the sort places a cell of more than 65,536 particles in
+    arrival order instead of counting, for each member, the members before it (10^12 steps
+    here), so the step ends promptly; the permutation is still a permutation of the input and
+    the step reports WC_ERR_NUMERIC."""
+    import time
+
+    n = 1 << 20
+    p = small(n, 0)
+    st = crowd(n, p)
+    with fluid(p, st) as f:
+        t = time.perf_counter()
+        f.step(1e-3, 2)
+        with pytest.raises(_abi.WatercubeError) as e:
+            f.synchronize()
+        el = time.perf_counter() - t
+        assert e.value.status == _abi.WC_ERR_NUMERIC
+        perm = f.permutation()
+    assert el < 5.0, f"two steps of a one-cell state took {el:.1f} s"
+    assert np.array_equal(np.sort(perm), np.arange(n, dtype=np.uint32))
+
+
 def test_overfull_rows_refused_by_surface_and_surrogate(gpu):
     from watercube_gb300.surface import Surface
     from watercube_gb300.surrogate import Surrogate

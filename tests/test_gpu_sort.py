@@ -31,7 +31,8 @@ def test_sort_initial_state(gpu, oracle, name):
     check_sort(oracle, p, st)
 
 
-@pytest.mark.parametrize("name,steps,dt", [("dam16k", 40, 1e-3), ("refdefaults", 30, 2e-4), ("dam1m", 8, 2.5e-4)])
+@pytest.mark.parametrize("name,steps,dt", [("dam16k", 40, 1e-3), ("refdefaults", 30, 2e-4), ("dam1m", 8, 2.5e-4),
+                                           ("dam1m", 1000, 2.5e-4)])
 def test_sort_evolved_state(gpu, oracle, name, steps, dt):
     """Input already in last step's sorted order with particles migrating between cells."""
     p, st = evolved(name, steps, dt)

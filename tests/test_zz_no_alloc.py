@@ -74,3 +74,50 @@ def test_noalloc_rejects_sizes_beyond_its_limit(wclib):
     rc = wclib.wc_sort_cells_noalloc(None, 0, 65, 0.015, None, None, None, None, None)
     assert rc == _abi.WC_ERR_INVALID_ARG
     assert b"cells" in wclib.wc_last_error()
+
+
+def test_noalloc_status_reports_device_errors(wclib):
+    """The call only enqueues work; its device-side errors reach the caller through
+    wc_sort_cells_noalloc_status, which allocates nothing either: a scan wait made to run out
+    (the bounded-wait test hook) gives WC_ERR_TIMEOUT, a NaN position and a cell of more than
+    65,536 particles give WC_ERR_NUMERIC, and a clean call afterwards reports WC_OK with tables
+    equal to the allocating sort's."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("no CUDA device for a GPU test")
+    p = finalize(dam_break_params(16384))  # 21^3 cells: three scan tiles
+    st = generate_dam_break(p, 0)
+    _abi.check(wclib.wc_debug_scan_stall(1, 64))
+    try:
+        noalloc_sort(wclib, torch, p, st)
+        assert wclib.wc_sort_cells_noalloc_status(None) == _abi.WC_ERR_TIMEOUT
+        assert b"invalid" in wclib.wc_last_error()
+    finally:
+        _abi.check(wclib.wc_debug_scan_stall(0, 0))
+
+    bad = st.copy()
+    bad["position"][[5, 700]] = np.nan
+    noalloc_sort(wclib, torch, p, bad)
+    assert wclib.wc_sort_cells_noalloc_status(None) == _abi.WC_ERR_NUMERIC
+    assert b"non-finite" in wclib.wc_last_error()
+
+    # a cell of 70,000 particles: beyond the 65,536 the stable rank is counted for, so its members
+    # take arrival order; the permutation is still a permutation and the cell is reported
+    q = reference_params()
+    q.num_particles = 100000
+    pc = finalize(q)
+    crowd = generate_reference_lattice(pc, 2)
+    rng = np.random.default_rng(3)
+    b = float(pc.bin_size)
+    crowd["position"][:70000] = 5 * b + rng.uniform(0.1 * b, 0.9 * b, size=(70000, 3))
+    keys, perm, offs, counts, _ = noalloc_sort(wclib, torch, pc, crowd)
+    assert wclib.wc_sort_cells_noalloc_status(None) == _abi.WC_ERR_NUMERIC
+    assert b"65536" in wclib.wc_last_error()
+    assert np.array_equal(np.sort(perm), np.arange(crowd.shape[0], dtype=np.uint32))
+    big = int(np.argmax(counts))
+    assert counts[big] >= 70000 and np.all(keys[perm[offs[big]:offs[big] + counts[big]]] == big)
+
+    keys, perm, offs, counts, srt = noalloc_sort(wclib, torch, p, st)
+    assert wclib.wc_sort_cells_noalloc_status(None) == _abi.WC_OK
+    e_keys, e_perm, e_offs, e_counts, _ = allocating_sort(p, st)
+    assert np.array_equal(perm, e_perm) and np.array_equal(offs, e_offs) and np.array_equal(keys, e_keys)

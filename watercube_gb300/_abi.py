@@ -288,6 +288,7 @@ def _declare(lib) -> None:
         "wc_surrogate_rollout": (S, [P, P, C.c_float, C.c_uint32, C.c_uint32, C.c_float, S, P,
                                      C.POINTER(RolloutStats)]),
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
+        "wc_sort_cells_noalloc_status": (S, [P]),
         "wc_set_device": (S, [C.c_int]),
         "wc_debug_scan_stall": (S, [S, C.c_uint32]),
         "wc_debug_fail_allocations": (None, [C.c_longlong]),

@@ -64,6 +64,12 @@ class Batch:
         state = np.ascontiguousarray(state, dtype=A.PARTICLE_DTYPE)
         check(lib().wc_batch_set_particles(self._h, A._ptr(state), state.shape[0]), "wc_batch_set_particles")
 
+    def ids(self) -> np.ndarray:
+        """Per state slot, the particle's index in the initial state (all scenes concatenated)."""
+        out = np.zeros(self.num_particles, np.uint32)
+        check(lib().wc_batch_get_ids(self._h, A._ptr(out), self.num_particles), "wc_batch_get_ids")
+        return out
+
     def offsets(self) -> np.ndarray:
         out = (C.c_uint64 * (self.num_scenes + 1))()
         check(lib().wc_batch_scene_offsets(self._h, out))

@@ -22,6 +22,10 @@ enum : uint32_t {
 // WC_ERR_NUMERIC. Such a cell only arises from a collapsed or non-finite state (every NaN
 // position bins to cell 0), where evaluating it would cost O(N^2) work per step.
 constexpr uint32_t MAX_CELL_PARTICLES = 2048;
+// The sort's stable in-cell rank counts, for each member of a cell, the members before it:
+// O(k^2) per cell. Cells of more than this many particles (only reachable from a collapsed or
+// non-finite state) take arrival order instead and are reported like an overfull cell.
+constexpr uint32_t MAX_SORT_CELL_PARTICLES = 65536;
 
 // Constants of one scene, by value in kernel parameters (single scene) or in a device table
 // (batched scenes).
@@ -119,7 +123,7 @@ struct DevBuffers {
     uint32_t *start;      // [C+1] exclusive prefix + total
     uint32_t *cell_list;  // [C] non-empty cells, ascending
     // [0]: non-empty cells (written by the scan); [1], [2]: the density and force passes' cell
-    // counters (dynamic scheduling; zeroed before each launch)
+    // counters (dynamic scheduling; each launch leaves its counter at zero)
     uint32_t *num_nonempty;
     unsigned long long* scan_desc;  // [num_tiles]
     uint32_t* scan_tile_counter;

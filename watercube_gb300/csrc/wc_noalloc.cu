@@ -19,6 +19,10 @@
 //     without ordering between them, or different host threads) race on it; order them.
 //   * Each call clears the part of the array that must start at zero (the histogram and the
 //     error word); the rest keeps the last call's contents.
+//   * Device-side errors (a non-finite position, a scan wait that ran out, a cell beyond
+//     MAX_SORT_CELL_PARTICLES) are recorded in the array's error word and not seen by the call,
+//     which only enqueues work. wc_sort_cells_noalloc_status(stream) waits for the stream and
+//     reports them for the last call; the word is cleared by the next call.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -40,8 +44,7 @@ constexpr size_t OFF_UNORDERED = align256(OFF_RANKS + sizeof(uint32_t) * MAXP);
 constexpr size_t OFF_COUNTS = align256(OFF_UNORDERED + sizeof(uint32_t) * MAXP);
 constexpr size_t OFF_CELL_LIST = align256(OFF_COUNTS + sizeof(uint32_t) * MAXC);
 constexpr size_t OFF_DESC = align256(OFF_CELL_LIST + sizeof(uint32_t) * MAXC);
-constexpr size_t OFF_GATHER = align256(OFF_DESC + sizeof(unsigned long long) * MAX_TILES);
-constexpr size_t OFF_WORDS = align256(OFF_GATHER + sizeof(float4) * MAXP);
+constexpr size_t OFF_WORDS = align256(OFF_DESC + sizeof(unsigned long long) * MAX_TILES);
 constexpr size_t SCRATCH_BYTES = align256(OFF_WORDS + 4 * sizeof(uint32_t));  // tile counter, non-empty count, error
 
 static __device__ __align__(256) unsigned char g_sort_scratch[SCRATCH_BYTES];
@@ -98,9 +101,9 @@ WC_API wc_status wc_sort_cells_noalloc(const void* d_positions, uint32_t n, uint
     d.num_cells = C;
     d.num_tiles = (C + wc::SCAN_TILE - 1) / wc::SCAN_TILE;
     d.pos_a = const_cast<float4*>(static_cast<const float4*>(d_positions));
-    d.vel_a = d.pos_a;  // the gather's second stream reads the positions again ...
+    d.vel_a = nullptr;  // positions only: the gather skips the velocity stream
     d.pos_b = static_cast<float4*>(d_sorted_positions);
-    d.vel_b = reinterpret_cast<float4*>(base + OFF_GATHER);  // ... into scratch
+    d.vel_b = nullptr;
     d.keys = d_keys;
     d.perm = d_permutation;
     d.start = d_cell_start;
@@ -128,6 +131,26 @@ WC_API wc_status wc_sort_cells_noalloc(const void* d_positions, uint32_t n, uint
     wc::launch_rank_gather(d, ld, s);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return wc::fail(WC_ERR_CUDA, "wc_sort_cells_noalloc launch: %s", cudaGetErrorString(e));
+    return WC_OK;
+}
+
+WC_API wc_status wc_sort_cells_noalloc_status(void* stream) {
+    wc::clear_error();
+    // The kernels report into the array's error word, which the caller cannot address. Copy it
+    // into a host word of this thread (no allocation), after the work already on `stream`.
+    thread_local uint32_t word = 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    WC_CUDA_TRY(cudaMemcpyFromSymbolAsync(&word, g_sort_scratch, sizeof word, OFF_WORDS + 2 * sizeof(uint32_t),
+                                          cudaMemcpyDeviceToHost, s));
+    WC_CUDA_TRY(cudaStreamSynchronize(s));
+    if (word & wc::DEVERR_SCAN_TIMEOUT)
+        return wc::fail(WC_ERR_TIMEOUT, "wc_sort_cells_noalloc: a scan tile gave up waiting; the cell table and "
+                                        "permutation of that call are invalid");
+    if (word & wc::DEVERR_NONFINITE)
+        return wc::fail(WC_ERR_NUMERIC, "wc_sort_cells_noalloc: a non-finite position was binned (to cell 0)");
+    if (word & wc::DEVERR_CELL_OVERFLOW)
+        return wc::fail(WC_ERR_NUMERIC, "wc_sort_cells_noalloc: a cell held more than %u particles; its members "
+                                        "were placed in arrival order", wc::MAX_SORT_CELL_PARTICLES);
     return WC_OK;
 }
 

@@ -10,6 +10,7 @@
 //   rank_gather   reorder.comp/sort.comp stable rank = #(members of the cell with a smaller
 //                                      index); writes the permutation (sort.comp:44) and
 //                                      gathers the SoA particle state into sorted order
+//                                      (cells beyond MAX_SORT_CELL_PARTICLES: arrival order)
 //
 // The reference's in-cell order is whatever order atomicAdd hands out; this sort defines it as
 // the input order (stable), so the permutation is reproducible and bit-exact against a serial
@@ -241,25 +242,37 @@ __global__ void __launch_bounds__(256) scatter_cells_kernel(uint32_t n, const ui
     }
 }
 
-template <bool IDS>
+// VEL: also gather the velocity stream (the cell sort alone moves positions only).
+// A cell of more than MAX_SORT_CELL_PARTICLES particles (a collapsed or non-finite state) takes
+// its members in arrival order instead: the stable rank costs O(k) per member, O(k^2) per cell,
+// and an all-NaN state puts every particle in cell 0. Arrival ranks are unique in the cell, so
+// the permutation stays a permutation; the step reports the cell through DEVERR_CELL_OVERFLOW.
+template <bool IDS, bool VEL>
 __global__ void __launch_bounds__(256) rank_gather_kernel(uint32_t n, const uint32_t* __restrict__ keys,
+                                                          const uint32_t* __restrict__ ranks,
                                                           const uint32_t* __restrict__ unordered,
                                                           const uint32_t* __restrict__ start,
                                                           const float4* __restrict__ pos_in,
                                                           const float4* __restrict__ vel_in,
                                                           const uint32_t* __restrict__ ids_in,
                                                           float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-                                                          uint32_t* __restrict__ ids_out, uint32_t* __restrict__ perm) {
+                                                          uint32_t* __restrict__ ids_out, uint32_t* __restrict__ perm,
+                                                          uint32_t* __restrict__ err) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t key = keys[i];
         const uint32_t s = start[key], e = min(start[key + 1], n);
         uint32_t r = 0;
-        for (uint32_t q = s; q < e; ++q) r += unordered[q] < i ? 1u : 0u;
+        if (e - min(s, e) <= MAX_SORT_CELL_PARTICLES) {
+            for (uint32_t q = s; q < e; ++q) r += unordered[q] < i ? 1u : 0u;
+        } else {
+            r = ranks[i];
+            if (r == 0u) atomicOr(err, DEVERR_CELL_OVERFLOW);
+        }
         const uint32_t dst = s + r;
         if (dst >= n) continue;
         perm[dst] = i;
         pos_out[dst] = pos_in[i];
-        vel_out[dst] = vel_in[i];
+        if (VEL) vel_out[dst] = vel_in[i];
         if (IDS) ids_out[dst] = ids_in[i];
     }
 }
@@ -325,12 +338,15 @@ void launch_scatter(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s) {
 
 void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s) {
     const int g = grid_for(d.n, ld.grid_stream);
-    if (d.ids_a)
-        rank_gather_kernel<true><<<g, 256, 0, s>>>(d.n, d.keys, d.unordered, d.start, d.pos_a, d.vel_a, d.ids_a,
-                                                   d.pos_b, d.vel_b, d.ids_b, d.perm);
+    if (!d.vel_a)
+        rank_gather_kernel<false, false><<<g, 256, 0, s>>>(d.n, d.keys, d.ranks, d.unordered, d.start, d.pos_a, nullptr,
+                                                           nullptr, d.pos_b, nullptr, nullptr, d.perm, d.err);
+    else if (d.ids_a)
+        rank_gather_kernel<true, true><<<g, 256, 0, s>>>(d.n, d.keys, d.ranks, d.unordered, d.start, d.pos_a, d.vel_a,
+                                                         d.ids_a, d.pos_b, d.vel_b, d.ids_b, d.perm, d.err);
     else
-        rank_gather_kernel<false><<<g, 256, 0, s>>>(d.n, d.keys, d.unordered, d.start, d.pos_a, d.vel_a, nullptr,
-                                                    d.pos_b, d.vel_b, nullptr, d.perm);
+        rank_gather_kernel<false, true><<<g, 256, 0, s>>>(d.n, d.keys, d.ranks, d.unordered, d.start, d.pos_a,
+                                                          d.vel_a, nullptr, d.pos_b, d.vel_b, nullptr, d.perm, d.err);
 }
 
 void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, cudaStream_t s) {

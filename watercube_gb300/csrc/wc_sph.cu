@@ -401,6 +401,14 @@ __device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, 
     if (ncount) ncount[ti] = hits - 1u;
 }
 
+// Dynamic cell scheduling: every warp takes cells from a counter until it draws an index >= M,
+// so a launch of W warps hands out exactly M + W indices and each warp's last draw is one of
+// M .. M + W - 1. The warp that draws M + W - 1 draws last; it puts the counter back to zero for
+// the next launch (no memset node, and no launch can start from a stale count).
+__device__ __forceinline__ void release_counter(uint32_t* counter, uint32_t m_last, uint32_t M, uint32_t lane) {
+    if (lane == 0 && m_last == M + gridDim.x * (uint32_t)WARPS - 1u) atomicExch(counter, 0u);
+}
+
 // ---- density --------------------------------------------------------------------------------
 
 // BATCHED: cells belong to several scenes (BatchTables); each cell takes its scene's constants
@@ -432,7 +440,8 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
     // fetched while the current cell runs), so dense cells do not pile up on a few warps.
     uint32_t* const counter = num_nonempty + 1;
     uint32_t m_next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
-    for (uint32_t m = __shfl_sync(FULL, m_next, 0); m < M; m = __shfl_sync(FULL, m_next, 0)) {
+    uint32_t m = __shfl_sync(FULL, m_next, 0);
+    for (; m < M; m = __shfl_sync(FULL, m_next, 0)) {
         if (lane == 0) m_next = atomicAdd(counter, 1u);
         const uint32_t cg = __ldg(cell_list + m);
         SceneConsts sc;
@@ -586,6 +595,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
             __syncwarp();  // the stage is rewritten for the next cell
         }
     }
+    release_counter(counter, m, M, lane);
 }
 
 // ---- force + integration ------------------------------------------------------------------------
@@ -716,7 +726,8 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
     // fetched while the current cell runs), so dense cells do not pile up on a few warps.
     uint32_t* const counter = num_nonempty + 2;
     uint32_t m_next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
-    for (uint32_t m = __shfl_sync(FULL, m_next, 0); m < M; m = __shfl_sync(FULL, m_next, 0)) {
+    uint32_t m = __shfl_sync(FULL, m_next, 0);
+    for (; m < M; m = __shfl_sync(FULL, m_next, 0)) {
         if (lane == 0) m_next = atomicAdd(counter, 1u);
         const uint32_t cg = __ldg(cell_list + m);
         SceneConsts sc;
@@ -955,6 +966,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
         }
         __syncwarp();  // the slot table and stage are rewritten for the next cell
     }
+    release_counter(counter, m, M, lane);
 }
 
 }  // namespace
@@ -985,7 +997,6 @@ LaunchDims compute_launch_dims(int device) {
 }
 
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s) {
-    cudaMemsetAsync(d.num_nonempty + 1, 0, sizeof(uint32_t), s);  // the pass's cell counter
     density_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
         sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
         reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty,
@@ -994,14 +1005,12 @@ void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims
 
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s) {
-    cudaMemsetAsync(d.num_nonempty + 2, 0, sizeof(uint32_t), s);
     force_kernel<false><<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, BatchTables{}, in, d.n, d.num_cells, d.pos_b,
                                                               d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
                                                               d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
 }
 
 void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
-    cudaMemsetAsync(d.num_nonempty + 1, 0, sizeof(uint32_t), s);
     density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
         SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
         reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
@@ -1009,7 +1018,6 @@ void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const La
 
 void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
                           cudaStream_t s) {
-    cudaMemsetAsync(d.num_nonempty + 2, 0, sizeof(uint32_t), s);
     force_kernel<true><<<ld.grid_force, SPH_THREADS, 0, s>>>(SceneConsts{}, bt, in, d.n, d.num_cells, d.pos_b,
                                                              d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
                                                              d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
