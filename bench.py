@@ -317,10 +317,27 @@ def run_reference(args):
     return 0
 
 
-def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01) -> dict:
-    """Plain SPH, surrogate, stale-acceleration and hybrid rollouts of `steps` steps from `st`, each
-    on a fresh fluid; the network uses the committed trained weights when present."""
+def by_id(f) -> np.ndarray:
+    """Positions of a fluid's state buffer in particle-id order."""
+    out = f.particles()
+    ids = f.particle_ids()
+    pos = np.empty((ids.size, 3))
+    pos[ids] = out["position"]
+    return pos
+
+
+def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01, gnn_steps: int = 8) -> dict:
+    """Rollouts of `steps` steps from `st`, each on a fresh fluid, against plain SPH over the same
+    steps: the learned fast rollout (cycles of one judge SPH step and K - 1 steps on the network's
+    accelerations) and the same cycles on the stale SPH acceleration (the method without the
+    network), with density error (the judge's), RMS and largest position drift from the plain
+    SPH trajectory (in h) and FP64 momentum / energy change; then the message-passing network's
+    judged modes, `gnn_steps` steps each (its step costs hundreds of plain steps at this size)."""
+    from watercube_gb300 import _abi
     from watercube_gb300.fluid import Fluid
+    from watercube_gb300.local import DEFAULT_WEIGHTS as LOCAL_WEIGHTS
+    from watercube_gb300.local import LocalNet, load_weights
+    from watercube_gb300.local import rollout as local_rollout
     from watercube_gb300.surrogate import (
         WC_ROLLOUT_HYBRID,
         WC_ROLLOUT_SPH,
@@ -329,32 +346,66 @@ def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01) -> 
         Surrogate,
         rollout,
     )
-    from watercube_gb300.train_surrogate import DEFAULT_WEIGHTS, load_weights
+    from watercube_gb300.train_surrogate import DEFAULT_WEIGHTS, load_weights as load_gnn
 
-    trained = DEFAULT_WEIGHTS.is_file()
-    s = load_weights() if trained else Surrogate(layers=8, seed=1)
-    out = {"steps": steps, "K": K, "tolerance": tolerance,
-           "weights": DEFAULT_WEIGHTS.relative_to(REPO).as_posix() if trained else "untrained (seed 1)"}
-    keep = ("particle_steps_per_s", "ms_device", "sph_steps", "surrogate_steps", "judged", "reverted",
+    q = p.copy()
+    q.flags |= _abi.WC_FLAG_TRACK_IDS
+    h = float(p.kernel_radius)
+    keep = ("particle_steps_per_s", "ms_device", "steps", "sph_steps", "surrogate_steps", "judged", "reverted",
             "mean_density_error", "max_density_error")
-    for mode, name in ((WC_ROLLOUT_SPH, "plain"), (WC_ROLLOUT_SURROGATE, "surrogate"), (WC_ROLLOUT_STALE, "stale"),
-                       (WC_ROLLOUT_HYBRID, "hybrid")):
-        f = Fluid.create("rollout", p)
-        f.setup(st)
-        # graph capture and workspace allocation outside the timed rollout
-        rollout(f, dt, 1 if mode == WC_ROLLOUT_SURROGATE else 2, K, tolerance, mode, s)
-        f.setup(st)
-        r = rollout(f, dt, steps, K, tolerance, mode, s)
+
+    def diag_changes(r):
         d0, d1 = np.array(r["diag_start"]), np.array(r["diag_end"])
-        e = {k: r[k] for k in keep}
-        e["momentum_change"] = float(np.linalg.norm(d1[1:4] - d0[1:4]))  # gravity and walls act on it
-        e["energy_change_rel"] = float(abs((d1[4] + d1[5]) - (d0[4] + d0[5])) / max(abs(d0[4] + d0[5]), 1e-30))
-        out[name] = e
-        f.close()
+        return {"momentum_change": float(np.linalg.norm(d1[1:4] - d0[1:4])),  # gravity and walls act on it
+                "energy_change_rel": float(abs((d1[4] + d1[5]) - (d0[4] + d0[5])) / max(abs(d0[4] + d0[5]), 1e-30))}
+
+    trained = LOCAL_WEIGHTS.is_file()
+    net = load_weights() if trained else LocalNet(ages=K - 1, seed=1)
+    out = {"steps": steps, "K": K, "tolerance": tolerance,
+           "weights": LOCAL_WEIGHTS.relative_to(REPO).as_posix() if trained else "untrained (seed 1)"}
+    with Fluid.create("rollout", q) as f:
+        f.setup(st)
+        f.step(dt, 2)
+        f.setup(st)
+        r = rollout(f, dt, steps, K, tolerance, WC_ROLLOUT_SPH, None)
+        plain_pos = by_id(f)
+        out["plain"] = {**{k: r[k] for k in keep}, **diag_changes(r)}
+    for name, model in (("learned", net), ("stale", None)):
+        with Fluid.create("rollout", q) as f:
+            f.setup(st)
+            local_rollout(f, dt, 2 * K, ages=K - 1, tolerance=tolerance, net=model)  # capture, workspaces
+            f.setup(st)
+            r = local_rollout(f, dt, steps, ages=K - 1, tolerance=tolerance, net=model)
+            d = np.linalg.norm(by_id(f) - plain_pos, axis=1) / h
+            e = {k: r[k] for k in keep}
+            e.update(diag_changes(r))
+            e["rms_drift_h"] = float(np.sqrt(np.mean(d * d)))
+            e["max_drift_h"] = float(d.max())
+            e["vs_plain"] = e["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
+            out[name] = e
+    net.close()
+    out["judge"] = ("every K-th step is plain SPH; it compares each particle's density carried through the "
+                    "skipped steps (the judge step's density plus its rate) with the SPH density of the same "
+                    "particles and reverts the cycle when the mean |rho_carried / rho_SPH - 1| exceeds the tolerance")
+    # the message-passing network (width 128, 8 layers) in its one-step-judged modes
+    gnn = {"steps": gnn_steps, "K": K}
+    trained_gnn = DEFAULT_WEIGHTS.is_file()
+    s = load_gnn() if trained_gnn else Surrogate(layers=8, seed=1)
+    gnn["weights"] = DEFAULT_WEIGHTS.relative_to(REPO).as_posix() if trained_gnn else "untrained (seed 1)"
+    for mode, name in ((WC_ROLLOUT_SURROGATE, "surrogate"), (WC_ROLLOUT_HYBRID, "hybrid"),
+                       (WC_ROLLOUT_STALE, "stale_one_step_judge")):
+        with Fluid.create("rollout", p) as f:
+            f.setup(st)
+            rollout(f, dt, 1 if mode == WC_ROLLOUT_SURROGATE else 2, K, tolerance, mode, s)
+            f.setup(st)
+            r = rollout(f, dt, gnn_steps, K, tolerance, mode, s)
+            e = {k: r[k] for k in keep}
+            e["vs_plain"] = e["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
+            gnn[name] = e
     s.close()
-    out["surrogate_vs_plain"] = out["surrogate"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
-    out["stale_vs_plain"] = out["stale"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
-    out["hybrid_vs_plain"] = out["hybrid"]["particle_steps_per_s"] / out["plain"]["particle_steps_per_s"]
+    out["message_passing"] = gnn
+    out["learned_vs_plain"] = out["learned"]["vs_plain"]
+    out["stale_vs_plain"] = out["stale"]["vs_plain"]
     return out
 
 
@@ -381,8 +432,9 @@ def run_surface(p, st, grid_res: int = 256, reps: int = 5) -> dict:
 
 
 def run_rollout_workload(args):
-    """--workload rollout1m: the judged rollouts at 1,048,576 particles from the dam break's initial
-    state, --steps steps each (dt = 2.5e-4, K = 4, 1% density tolerance)."""
+    """--workload rollout1m: the rollouts at 1,048,576 particles from the dam break's initial
+    state (dt = 2.5e-4, K = 4, 1% density tolerance), --steps steps each (default 2,000, the
+    workload's length); the value is the learned fast rollout's particle-steps/s."""
     from watercube_gb300 import _abi
     from watercube_gb300.fluid import dam_break_params, finalize, generate_dam_break
 
@@ -392,20 +444,22 @@ def run_rollout_workload(args):
     st = generate_dam_break(p, 0)
     with Clocks(0) as clocks:
         r = run_rollouts(p, st, dt, args.steps)
+    learned = r["learned"]
     line = {
-        "metric": "particle-steps/s at 1M particles, surrogate-assisted rollout (K=4, 1% density tolerance)",
-        "value": r["surrogate"]["particle_steps_per_s"],
+        "metric": "particle-steps/s at 1M particles, learned rollout (K=4, 1% density tolerance)",
+        "value": learned["particle_steps_per_s"],
         "unit": UNIT,
         "n_gpus": 1,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": r["surrogate"]["ms_device"] / args.steps,
+        "ms_per_step": learned["ms_device"] / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 solver, bf16 network (fp32 accumulate)",
         "data": "synthetic",
-        "config": {"workload": desc + ", rollout from the initial state", "particles": n, "dt": dt},
+        "config": {"workload": desc + ", rollout from the initial state", "particles": n, "dt": dt, "K": 4,
+                   "tolerance": 0.01},
         "rollout": r,
         "clocks": clocks.summary(),
     }
@@ -552,28 +606,78 @@ def run_ours(args):
     return 0
 
 
+def batch_cpu_baseline(specs, params, states, dt, threads_all: int, scenes: int = 8, steps: int = 2) -> dict:
+    """The oracle's FP32 transcription on a bounded sample of the batched workload: `steps` full
+    steps of `scenes` scenes spread over the draw (every 64th), all threads, per scene in turn."""
+    from oracle.oracle import Oracle
+
+    o = Oracle()
+    pick = list(range(0, len(specs), max(1, len(specs) // scenes)))[:scenes]
+    n = 0
+    el = 0.0
+    for s in pick:
+        st = states[s].copy()
+        o.step(params[s], st, dt, 1, threads=threads_all)  # page-in, thread pool
+        t = time.perf_counter()
+        o.step(params[s], st, dt, steps, threads=threads_all)
+        el += time.perf_counter() - t
+        n += st.shape[0] * steps
+    return {"value": n / el, "unit": UNIT, "cores": threads_all, "kind": "port",
+            "sample": f"{steps} full steps of each of {len(pick)} scenes (every {max(1, len(specs) // scenes)}th of the "
+                      f"512-scene draw, {n // steps} particles), one scene at a time on all threads, after one "
+                      "warm-up step: the oracle's FP32 transcription of the reference's shader stages"}
+
+
 def run_batch(args):
     """The 512-scene batched workload (4,096-65,536 particles per scene, log-uniform, seed 0):
-    autotuned, then timed like the single-scene step."""
+    autotuned, then timed like the single-scene step; the scenes' SPH arithmetic is the plain
+    step's, so the same algorithmic bytes per particle-step apply."""
     from watercube_gb300 import _abi
-    from watercube_gb300.batch import Batch, batch_specs
+    from watercube_gb300.batch import Batch, batch_specs, scene_params, scene_particles
+    from watercube_gb300.fluid import PinnedBuffer
 
     _abi.check(_abi.lib().wc_set_device(0), "select device")
     specs = batch_specs(512, 4096, 65536, seed=0)
     dt = 1e-3
-    b = Batch.from_specs(specs)
+    params = [scene_params(x) for x in specs]
+    states = [scene_particles(x, q) for x, q in zip(specs, params)]
+    b = Batch(params, states)
     n = b.num_particles
     t0 = time.perf_counter()
     tuning = b.tune(dt)
     tune_s = time.perf_counter() - t0
-    b.step(dt, max(args.warmup, 3))
+    warm = max(args.warmup, 3)
+    b.step(dt, warm)
     with Clocks(0) as clocks:
         ms = b.time_steps(dt, args.steps, flush_l2=True)
     total_ms = float(ms.sum())
     d = b.diagnostics()
+    value = n * args.steps / (total_ms * 1e-3)
+    peak, peak_kind = measured_peaks()
+    cells = sum(int(q.grid_res) ** 3 for q in params)
+    step_gbs = step_algo_bytes(n, cells) * n / (total_ms / args.steps * 1e-3) / 1e9
+
+    # end to end through the public API with host buffers (pinned), the same number of steps
+    # from the same state: upload every scene's particles, step, read them back
+    state0 = b.particles()
+    nbytes = n * 32
+    hin, hout = PinnedBuffer(nbytes), PinnedBuffer(nbytes)
+    ain, aout = hin.particles(n), hout.particles(n)
+    lib = _abi.lib()
+    b.set_particles(states_concat(states))
+    b.step(dt, warm)
+    ain[:] = b.particles()
+    e2e_steps = min(args.steps, 100)
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        _abi.check(lib.wc_batch_set_particles(b._h, ain.ctypes.data, n))
+        _abi.check(lib.wc_batch_step(b._h, dt, 1))
+        _abi.check(lib.wc_batch_get_particles(b._h, aout.ctypes.data, n))
+        ain, aout = aout, ain
+    el = time.perf_counter() - t
     line = {
         "metric": "particle-steps/s, 512 batched scenes (plain SPH step)",
-        "value": n * args.steps / (total_ms * 1e-3),
+        "value": value,
         "unit": UNIT,
         "n_gpus": 1,
         "steps": args.steps,
@@ -584,33 +688,51 @@ def run_batch(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "512 scenes, 4,096-65,536 particles each (log-uniform), dt=1e-3", "particles": n,
+        "config": {"workload": "512 scenes, 4,096-65,536 particles each (log-uniform, seed 0), random blocks, "
+                               "v ~ N(0, 0.5), k ~ U[2, 6], dt=1e-3", "particles": n, "cells": cells,
+                   "window": f"steps {warm + 1} .. {warm + args.steps} from the initial states",
                    "l2": "flushed before every timed step (read of 2x L2), outside the timed span"},
+        "roofline": {"bound": "hbm", "kernel": "whole step", "achieved": step_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": step_gbs / peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                     "algorithmic_bytes_per_particle": step_algo_bytes(n, cells), "traffic": None},
         "tuning": {"density_blocks_per_sm": tuning.density_blocks_per_sm,
                    "force_blocks_per_sm": tuning.force_blocks_per_sm,
                    "stream_blocks_per_sm": tuning.stream_blocks_per_sm, "cell_factor": tuning.cell_factor,
                    "trials": tuning.trials, "tune_seconds": tune_s},
+        "e2e": {"value": n * e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps,
+                "pattern": "wc_batch_set_particles(pinned host) + wc_batch_step + wc_batch_get_particles(pinned host)"},
         "gpu_launches": 6 * args.steps,
         "clocks": clocks.summary(),
         "mass_total": float(d[:, 0].sum()),
     }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = batch_cpu_baseline(specs, params, states, dt, os.cpu_count() or 1)
+    del state0
     b.close()
+    hin.free()
+    hout.free()
     print(json.dumps(line))
     return 0
+
+
+def states_concat(states):
+    return np.concatenate(states)
 
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default: 1000 for the single scenes, 200 for batch512, 16 for rollout1m; "
+                    help="timed steps (default: 1000 for the single scenes, 500 for batch512, 2000 for rollout1m; "
                          "20 for --impl reference)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512", "rollout1m"], default="dam1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-rollout", action="store_true")
-    ap.add_argument("--rollout-steps", type=int, default=8)
+    ap.add_argument("--rollout-steps", type=int, default=200)
     ap.add_argument("--advance", type=int, default=0, help="untimed steps before the warm-up (single scenes)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -619,7 +741,7 @@ def main():
         if args.impl == "reference":
             args.steps = 20
         else:
-            args.steps = {"batch512": 200, "rollout1m": 16}.get(args.workload, 1000)
+            args.steps = {"batch512": 500, "rollout1m": 2000}.get(args.workload, 1000)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch512":

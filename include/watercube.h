@@ -75,7 +75,11 @@ enum {
        of the Spiky kernel over the wall plane). No counterpart in the reference: the
        replacement for its pseudo wall density and force that its report names as the next
        physics fix. */
-    WC_FLAG_WALL_WEIGHTS = 1u << 6
+    WC_FLAG_WALL_WEIGHTS = 1u << 6,
+    /* Run the force pass as one 32-lane team per non-empty cell (WC_FORCE_TEAM) instead of one
+       lane per target (the default, WC_FORCE_LANE); the same neighbour sets, the sums differ
+       only in the order of their additions. */
+    WC_FLAG_FORCE_TEAM = 1u << 7
 };
 
 /* The reference's four active behaviours. */
@@ -313,6 +317,11 @@ WC_API void wc_batch_destroy(wc_batch* b);
 
 /* Launch geometry the autotuner picks: resident blocks per SM of the two neighbour passes and
    of the per-particle kernels, and the cell edge as a multiple of each scene's h. */
+/* Force pass variants (threads per cell): one 32-lane team per non-empty cell, its targets split
+   into slices, or one lane per target. Same neighbour sets; sums differ in addition order only. */
+#define WC_FORCE_TEAM 0
+#define WC_FORCE_LANE 1
+
 typedef struct wc_tuning {
     uint32_t density_blocks_per_sm;
     uint32_t force_blocks_per_sm;
@@ -320,6 +329,7 @@ typedef struct wc_tuning {
     float cell_factor;
     float step_ms; /* best measured step time */
     uint32_t trials;
+    uint32_t force_variant; /* WC_FORCE_TEAM or WC_FORCE_LANE */
 } wc_tuning;
 
 /* Time graph replays of candidate geometries (the state is saved before and restored after,
@@ -501,6 +511,66 @@ typedef struct wc_rollout_stats {
    velocity history; NULL starts it as five copies of the current velocity. */
 WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t K,
                                       float tolerance, int mode, const float* hist, wc_rollout_stats* stats);
+
+/* ---- learned fast rollout (no counterpart in the reference) ------------------------------ */
+/*
+ * A per-particle network that predicts the SPH acceleration of the next K-1 steps from sums
+ * the SPH step computes anyway. Every K-th step is a plain SPH step (the judge); its force pass
+ * also accumulates, per particle, the time derivative of the pair terms under the neighbours'
+ * relative motion (J) and the Poly6 density rate. The network maps 19 per-particle inputs
+ * (the SPH acceleration, J dt, the density rate, velocity, density, pressure, six wall
+ * distances, k / rho0) through two hidden layers of 64 (ReLU) to the acceleration changes of
+ * ages 1 .. K-1, on the tensor cores (BF16 operands, FP32 accumulation in tensor memory). The
+ * skipped steps integrate a(t) + change without sorting, and carry each particle's density by
+ * its rate. The judge compares that carried density with the SPH density the next judge step
+ * computes for the same particles; a cycle whose mean |rho_carried / rho_SPH - 1| exceeds the
+ * tolerance is reverted: its K-1 steps are recomputed by plain SPH from the state after the
+ * previous judge step.
+ */
+typedef struct wc_local wc_local;
+
+typedef struct wc_local_config {
+    uint32_t ages;        /* K - 1: predicted ages, 1 .. 4 */
+    uint32_t seed;        /* weight initialisation */
+    float accel_scale;    /* accelerations are learned in units of this (m/s^2) */
+    float velocity_scale; /* velocities enter in units of this (m/s) */
+    uint64_t capacity;    /* training samples kept on the device (rows) */
+} wc_local_config;
+
+WC_API void wc_local_config_default(wc_local_config* c);
+WC_API wc_status wc_local_create(const wc_local_config* c, wc_local** out);
+WC_API void wc_local_destroy(wc_local* net);
+WC_API uint64_t wc_local_num_params(const wc_local* net);
+WC_API wc_status wc_local_get_params(wc_local* net, float* out, uint64_t count);
+WC_API wc_status wc_local_set_params(wc_local* net, const float* in, uint64_t count);
+/* Record training samples from `cycles` cycles of plain SPH on a fluid (needs
+   WC_FLAG_TRACK_IDS) or a batch: at each cycle's first step the inputs, then the SPH
+   accelerations of the next `ages` steps, matched by particle id. The fluid or batch advances
+   (ages + 1) * cycles steps. Samples go to the training set, or to the held-out set. */
+WC_API wc_status wc_local_record_fluid(wc_local* net, wc_fluid* f, float dt, uint32_t cycles, int held_out);
+WC_API wc_status wc_local_record_batch(wc_local* net, wc_batch* b, float dt, uint32_t cycles, int held_out);
+WC_API uint64_t wc_local_num_samples(const wc_local* net, int held_out);
+WC_API wc_status wc_local_clear_samples(wc_local* net);
+/* Adam on the mean squared error over the predicted ages, minibatches of `rows` training samples
+   drawn with a fixed generator; loss (optional, host [steps]) gets each step's loss. */
+WC_API wc_status wc_local_train(wc_local* net, uint32_t steps, uint32_t rows, float lr, float* loss);
+/* Test hook: the loss and the gradient of every parameter ([wc_local_num_params]) on the
+   training samples with the given row indices (modulo the sample count), without an update. */
+WC_API wc_status wc_local_gradients(wc_local* net, const uint32_t* rows_idx, uint32_t rows, float* grads, float* loss);
+/* Copy samples [first, first + count) of a set: inputs [count][32] and targets [count][16]
+   (acceleration changes / accel_scale; 3 per age); either pointer may be NULL. */
+WC_API wc_status wc_local_get_samples(wc_local* net, int held_out, uint64_t first, uint64_t count, float* inputs,
+                                      float* targets);
+/* Relative L2 error of the network's prediction of the acceleration at each age, and of the
+   stale acceleration (the method without the network), over a sample set: host [ages] each. */
+WC_API wc_status wc_local_evaluate(wc_local* net, int held_out, float* err_net, float* err_stale);
+/* The network's outputs (acceleration changes, [n][4 * ages] floats, host) for the fluid's
+   current state: one judge step's inputs without advancing it (test hook of the inference). */
+WC_API wc_status wc_local_predict(wc_local* net, wc_fluid* f, float dt, float* inputs, float* outputs);
+/* Advance the fluid nsteps as cycles of one judge SPH step and `ages` steps on predicted
+   accelerations (net = NULL: the stale SPH acceleration, the method without the network). */
+WC_API wc_status wc_local_rollout(wc_local* net, wc_fluid* f, float dt, uint32_t nsteps, uint32_t ages,
+                                  float tolerance, wc_rollout_stats* stats);
 
 /* ---- cell sort without allocation ------------------------------------------------------ */
 

@@ -35,6 +35,9 @@ WC_FLAG_MOUSE_FORCE = 1 << 3
 WC_FLAG_TRACK_IDS = 1 << 4
 WC_FLAG_NEIGHBOR_COUNTS = 1 << 5
 WC_FLAG_WALL_WEIGHTS = 1 << 6
+WC_FLAG_FORCE_TEAM = 1 << 7
+WC_FORCE_TEAM = 0
+WC_FORCE_LANE = 1
 WC_FLAGS_REFERENCE = WC_FLAG_WALL_DENSITY | WC_FLAG_WALL_FORCE | WC_FLAG_SPEED_CLAMP | WC_FLAG_MOUSE_FORCE
 
 WC_BUFFER_STATE = 1
@@ -134,6 +137,17 @@ class Tuning(C.Structure):
         ("cell_factor", C.c_float),
         ("step_ms", C.c_float),
         ("trials", C.c_uint32),
+        ("force_variant", C.c_uint32),
+    ]
+
+
+class LocalConfig(C.Structure):
+    _fields_ = [
+        ("ages", C.c_uint32),
+        ("seed", C.c_uint32),
+        ("accel_scale", C.c_float),
+        ("velocity_scale", C.c_float),
+        ("capacity", C.c_uint64),
     ]
 
 
@@ -287,6 +301,22 @@ def _declare(lib) -> None:
         "wc_surrogate_adam": (S, [P, C.c_float, C.c_float]),
         "wc_surrogate_rollout": (S, [P, P, C.c_float, C.c_uint32, C.c_uint32, C.c_float, S, P,
                                      C.POINTER(RolloutStats)]),
+        "wc_local_config_default": (None, [C.POINTER(LocalConfig)]),
+        "wc_local_create": (S, [C.POINTER(LocalConfig), C.POINTER(P)]),
+        "wc_local_destroy": (None, [P]),
+        "wc_local_num_params": (C.c_uint64, [P]),
+        "wc_local_get_params": (S, [P, P, C.c_uint64]),
+        "wc_local_set_params": (S, [P, P, C.c_uint64]),
+        "wc_local_record_fluid": (S, [P, P, C.c_float, C.c_uint32, C.c_int]),
+        "wc_local_record_batch": (S, [P, P, C.c_float, C.c_uint32, C.c_int]),
+        "wc_local_num_samples": (C.c_uint64, [P, C.c_int]),
+        "wc_local_clear_samples": (S, [P]),
+        "wc_local_train": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P]),
+        "wc_local_gradients": (S, [P, P, C.c_uint32, P, P]),
+        "wc_local_get_samples": (S, [P, C.c_int, C.c_uint64, C.c_uint64, P, P]),
+        "wc_local_evaluate": (S, [P, C.c_int, P, P]),
+        "wc_local_predict": (S, [P, P, C.c_float, P, P]),
+        "wc_local_rollout": (S, [P, P, C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.POINTER(RolloutStats)]),
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_sort_cells_noalloc_status": (S, [P]),
         "wc_set_device": (S, [C.c_int]),

@@ -190,6 +190,12 @@ wc_status apply_cell_factor(wc_batch* b, float factor) {
 }
 
 void apply_geometry(wc_batch* b, const wc_tuning& t) {
+    const int variant = t.force_variant == WC_FORCE_TEAM ? FORCE_TEAM : FORCE_LANE;
+    if (variant != b->ld.force_variant) {
+        b->ld.force_variant = variant;
+        sph_occupancy(true, &b->max_density_blocks, &b->max_force_blocks, variant);
+    }
+    b->tuning.force_variant = (uint32_t)variant;
     b->ld.grid_density = b->ld.sms * (int)std::max(1u, std::min(t.density_blocks_per_sm, (uint32_t)b->max_density_blocks));
     b->ld.grid_force = b->ld.sms * (int)std::max(1u, std::min(t.force_blocks_per_sm, (uint32_t)b->max_force_blocks));
     b->ld.grid_stream = b->ld.sms * (int)std::max(1u, t.stream_blocks_per_sm);
@@ -227,7 +233,7 @@ wc_status capture(wc_batch* b, const StepInputs& in) {
         if (ty != cudaGraphNodeTypeKernel) continue;
         cudaKernelNodeParams kp;
         WC_CUDA_TRY(cudaGraphKernelNodeGetParams(nd, &kp));
-        if (kp.func == force_kernel_batched_symbol()) {
+        if (kp.func == force_kernel_batched_symbol(b->ld.force_variant)) {
             b->force_node = nd;
             b->force_params = kp;
         }
@@ -350,12 +356,12 @@ bool cache_lookup(const TuneKey& k, wc_tuning* out) {
     FILE* f = std::fopen(path.c_str(), "r");
     if (!f) return false;
     unsigned long long n, c;
-    unsigned d, fo, st;
+    unsigned d, fo, st, fv;
     float cf, ms;
     bool found = false;
-    while (std::fscanf(f, "%llu %llu %u %u %u %f %f", &n, &c, &d, &fo, &st, &cf, &ms) == 7) {
+    while (std::fscanf(f, "%llu %llu %u %u %u %f %f %u", &n, &c, &d, &fo, &st, &cf, &ms, &fv) == 8) {
         if (n == k.n && c == k.cells) {
-            *out = wc_tuning{d, fo, st, cf, ms, 0};
+            *out = wc_tuning{d, fo, st, cf, ms, 0, fv};
             found = true;
         }
     }
@@ -371,12 +377,39 @@ void cache_store(const TuneKey& k, const wc_tuning& t) {
     if (path.empty()) return;
     FILE* f = std::fopen(path.c_str(), "a");
     if (!f) return;
-    std::fprintf(f, "%llu %llu %u %u %u %.3f %.6f\n", (unsigned long long)k.n, (unsigned long long)k.cells,
-                 t.density_blocks_per_sm, t.force_blocks_per_sm, t.stream_blocks_per_sm, t.cell_factor, t.step_ms);
+    std::fprintf(f, "%llu %llu %u %u %u %.3f %.6f %u\n", (unsigned long long)k.n, (unsigned long long)k.cells,
+                 t.density_blocks_per_sm, t.force_blocks_per_sm, t.stream_blocks_per_sm, t.cell_factor, t.step_ms,
+                 t.force_variant);
     std::fclose(f);
 }
 
 }  // namespace
+
+namespace wc {
+
+StepTarget batch_target(wc_batch* b) {
+    StepTarget t{};
+    t.d = &b->d;
+    t.bt = tables(b);
+    t.in = &b->in;
+    t.ld = b->ld;
+    t.stream = b->stream;
+    t.batch = b;
+    return t;
+}
+
+wc_status batch_graph_step(wc_batch* b, float dt) {
+    b->in.dt = dt;
+    return launch(b, b->in);
+}
+
+wc_status batch_check(wc_batch* b) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(WC_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    return read_errors(b);
+}
+
+}  // namespace wc
 
 extern "C" {
 
@@ -523,11 +556,15 @@ WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, w
         cudaMemsetAsync(d.num_nonempty, 0, 3 * sizeof(uint32_t), b->stream);
         cudaMemsetAsync(d.start, 0, sizeof(uint32_t) * (cells + 1), b->stream);
         if (n) cudaMemsetAsync(d.hits, 0, sizeof(uint32_t) * MASK_WORDS * (size_t)n, b->stream);
-        b->ld = compute_launch_dims(b->device);
-        sph_occupancy(true, &b->max_density_blocks, &b->max_force_blocks);
+        // the force pass variant of the scenes' flags (a fluid with the same flags gives each scene's
+        // result bit for bit)
+        const int variant = (b->base[0].flags & WC_FLAG_FORCE_TEAM) ? FORCE_TEAM : FORCE_LANE;
+        b->ld = compute_launch_dims(b->device, variant);
+        sph_occupancy(true, &b->max_density_blocks, &b->max_force_blocks, variant);
         b->ld.grid_density = b->ld.sms * b->max_density_blocks;
         b->ld.grid_force = b->ld.sms * b->max_force_blocks;
-        b->tuning = wc_tuning{(uint32_t)b->max_density_blocks, (uint32_t)b->max_force_blocks, 8u, 1.0f, 0.f, 0u};
+        b->tuning = wc_tuning{(uint32_t)b->max_density_blocks, (uint32_t)b->max_force_blocks, 8u, 1.0f, 0.f, 0u,
+                              (uint32_t)variant};
         b->in = make_step_inputs(b->base[0], 0.0f);
         st = apply_cell_factor(b, 1.0f);
     }
@@ -760,6 +797,18 @@ WC_API wc_status wc_batch_tune(wc_batch* b, float dt, wc_tuning* out) {
         wc_tuning t = best;
         t.density_blocks_per_sm = (uint32_t)blocks;
         WC_TRY(trial(t));
+    }
+    // threads per cell of the force pass: a 32-lane team per cell or one lane per target, each
+    // at its own largest residency
+    for (uint32_t variant : {(uint32_t)WC_FORCE_LANE, (uint32_t)WC_FORCE_TEAM}) {
+        wc_tuning t = best;
+        t.force_variant = variant;
+        t.force_blocks_per_sm = 64;  // clamped to the variant's occupancy
+        WC_TRY(trial(t));
+    }
+    {
+        wc_tuning probe = best;
+        WC_TRY(wc_batch_set_tuning(b, &probe));  // max_force_blocks of the chosen variant
     }
     for (int blocks = b->max_force_blocks; blocks >= 1; --blocks) {
         wc_tuning t = best;

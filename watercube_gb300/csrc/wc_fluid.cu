@@ -155,7 +155,7 @@ wc_status capture_graph(wc_fluid* f, const StepInputs& in) {
     WC_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &count));
     std::vector<cudaGraphNode_t> nodes(count);
     WC_CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &count));
-    const void* force_fn = force_kernel_symbol(f->params.flags);
+    const void* force_fn = force_kernel_symbol(f->ld.force_variant);
     for (cudaGraphNode_t nd : nodes) {
         cudaGraphNodeType ty;
         WC_CUDA_TRY(cudaGraphNodeGetType(nd, &ty));
@@ -241,6 +241,22 @@ FluidInternals fluid_internals(wc_fluid* f) {
 
 void fluid_enqueue_sort(wc_fluid* f) { enqueue_sort(f); }
 
+StepTarget fluid_target(wc_fluid* f) {
+    StepTarget t{};
+    t.d = &f->d;
+    t.sc = f->sc;
+    t.in = &f->in;
+    t.ld = f->ld;
+    t.stream = f->stream;
+    t.fluid = f;
+    return t;
+}
+
+wc_status fluid_check(wc_fluid* f) {
+    WC_TRY(check_launch());
+    return read_device_errors(f);
+}
+
 wc_status fluid_graph_step(wc_fluid* f, float dt) {
     // the caller counts its own steps (a judged rollout step runs this and a candidate)
     const uint64_t steps = f->steps;
@@ -282,7 +298,7 @@ WC_API wc_status wc_fluid_create(const wc_params* p, wc_fluid** out) {
         delete f;
         return s;
     }
-    f->ld = compute_launch_dims(f->device);
+    f->ld = compute_launch_dims(f->device, (f->params.flags & WC_FLAG_FORCE_TEAM) ? FORCE_TEAM : FORCE_LANE);
     f->sc = make_scene_consts(prm);
     f->in = make_step_inputs(prm, 0.0f);
     *out = f;

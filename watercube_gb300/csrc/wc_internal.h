@@ -66,6 +66,24 @@ __host__ __device__ __forceinline__ uint32_t div_R(uint32_t n, uint32_t R, uint3
     return q;
 }
 
+#ifdef __CUDACC__
+// The cell of a position: ivec3(p / binSize) clamped to [0, R-1] per axis (count.comp:31-33),
+// IEEE division, NaN -> 0; the sort's binning, so any kernel recomputing a particle's cell from
+// its (sorted) position finds the cell the sort put it in.
+__device__ __forceinline__ int32_t bin_axis(float q, int32_t R) {
+    if (!(q >= 1.0f)) return 0;
+    if (q >= (float)(R - 1)) return R - 1;
+    return (int32_t)q;
+}
+__device__ __forceinline__ uint32_t bin_key(float x, float y, float z, float bin, int32_t R, int32_t* cx, int32_t* cy,
+                                            int32_t* cz) {
+    *cx = bin_axis(__fdiv_rn(x, bin), R);
+    *cy = bin_axis(__fdiv_rn(y, bin), R);
+    *cz = bin_axis(__fdiv_rn(z, bin), R);
+    return (uint32_t)((*cz * R + *cy) * R + *cx);
+}
+#endif
+
 // Scene tables of a batch of independent scenes in one set of buffers (device memory). Scene s
 // owns particle slots [poff[s], poff[s+1]) and cell keys [coff[s], coff[s] + R_s^3); one global
 // counting sort over all keys therefore keeps every scene inside its own slot range.
@@ -133,15 +151,22 @@ struct DevBuffers {
     uint32_t* err;
 };
 
+// Force pass variants (threads per cell): a 32-lane team per non-empty cell that splits the
+// cell's targets into slices (FORCE_TEAM), or one lane per target (FORCE_LANE). Both replay the
+// density pass's neighbour bit strings and give the same neighbour sets; their sums differ only
+// in the order of the additions.
+enum : int { FORCE_TEAM = 0, FORCE_LANE = 1 };
+
 // Launch geometry computed once per handle.
 struct LaunchDims {
     int sms;
     int grid_stream;   // blocks for the per-particle kernels
     int grid_density;  // persistent blocks
     int grid_force;
+    int force_variant;
 };
 
-LaunchDims compute_launch_dims(int device);
+LaunchDims compute_launch_dims(int device, int force_variant = FORCE_LANE);
 
 // Stage launchers (wc_sort.cu, wc_sph.cu). All enqueue on `s` and never synchronise.
 void launch_bin_count(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
@@ -151,6 +176,12 @@ void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t 
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s);
+// The force pass of a learned-rollout judge step: as launch_force(_batched), and per particle
+// feat[ti] = (d a/dt under the neighbours' relative motion, density rate) in sorted order.
+void launch_force_feat(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
+                       float4* feat, cudaStream_t s);
+void launch_force_batched_feat(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
+                               float4* feat, cudaStream_t s);
 // AoS <-> SoA for host copies through a contiguous staging buffer.
 void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, cudaStream_t s);
 void launch_soa_to_aos(const float4* pos, const float4* vel, float4* aos, uint32_t n, cudaStream_t s);
@@ -183,19 +214,21 @@ struct ForceKernelArgs {
     const uint32_t* hits;
     float4* accel;
     uint32_t* err;
-    void* ptrs[17];
+    float4* feat = nullptr;  // the feature output of the learned rollout's judge steps (unused here)
+    static constexpr int COUNT = 18;  // every parameter of force_kernel, in order
+    void* ptrs[COUNT];
     void bind() {
-        void* p[17] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b, &pos_a,
-                       &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits, &accel, &err};
-        for (int i = 0; i < 17; ++i) ptrs[i] = p[i];
+        void* p[COUNT] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b, &pos_a,
+                          &vel_a, &ids_a, &start, &cell_list, &num_nonempty, &hits, &accel, &err, &feat};
+        for (int i = 0; i < COUNT; ++i) ptrs[i] = p[i];
     }
 };
 
 // The kernel entry points the force node of a captured graph is recognised by.
-const void* force_kernel_symbol(uint32_t flags);
-const void* force_kernel_batched_symbol();
+const void* force_kernel_symbol(int force_variant);
+const void* force_kernel_batched_symbol(int force_variant);
 // Resident blocks per SM of the two neighbour passes (single-scene or batched variant).
-void sph_occupancy(bool batched, int* density_blocks, int* force_blocks);
+void sph_occupancy(bool batched, int* density_blocks, int* force_blocks, int force_variant);
 
 // Internals of a wc_fluid, for the surrogate (wc_surrogate.cu), which works on a fluid's buffers.
 struct FluidInternals {
@@ -206,6 +239,27 @@ struct FluidInternals {
     cudaStream_t stream;
 };
 FluidInternals fluid_internals(wc_fluid* f);
+
+// A fluid or a batch of scenes as the learned rollout and its sample recorder drive them: the
+// buffers, the constants (sc for a fluid; bt.num_scenes > 0 for a batch), the step inputs and
+// the stream. Exactly one of fluid and batch is set.
+struct StepTarget {
+    DevBuffers* d;
+    SceneConsts sc;
+    BatchTables bt;
+    StepInputs* in;
+    LaunchDims ld;
+    cudaStream_t stream;
+    wc_fluid* fluid;
+    wc_batch* batch;
+};
+StepTarget fluid_target(wc_fluid* f);
+StepTarget batch_target(wc_batch* b);
+wc_status batch_graph_step(wc_batch* b, float dt);  // one plain step (graph replay)
+wc_status batch_check(wc_batch* b);                 // launch errors and device error word
+wc_status fluid_check(wc_fluid* f);
+// FP64 totals of a fluid's state buffer: mass, momentum x/y/z, kinetic and potential energy.
+wc_status fluid_diagnostics(wc_fluid* f, double out[6]);
 void fluid_enqueue_sort(wc_fluid* f);
 wc_status fluid_graph_step(wc_fluid* f, float dt);  // one plain SPH step (graph replay)
 void fluid_count_step(wc_fluid* f);

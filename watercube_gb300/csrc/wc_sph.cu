@@ -600,10 +600,19 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
 
 // ---- force + integration ------------------------------------------------------------------------
 
+// Accumulators of the force pass per target: NF_PLAIN for the step; with FEAT also the time
+// derivative of the pair terms under the pair's relative motion, and the density rate.
+constexpr int NF_PLAIN = 6, NF_FEAT = 13;
+
 // One neighbour's pressure and viscosity terms. f[0..2] collects pres*(h-d)^2*r/d and f[3..5]
 // collects (v_j - v_i)*(h-d)/rho_j; the constant factors are applied once per particle.
+// FEAT (the learned rollout's judge steps): with u = v_i - v_j the rate of r, and d' = r.u/d the
+// rate of d, f[6..8] collects d/dt of the pressure term at fixed pressures and densities,
+// (dcoef/dd) d' r + coef u, f[9..11] that of the viscosity term, (v_j - v_i)(-d')/rho_j, and
+// f[12] the Poly6 density rate sum (cull - d2)^2 (r.u) (times -6 m c6 per particle).
+template <bool FEAT = false>
 __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, const float4& pj, const float4& vj,
-                                           float h, float f[6]) {
+                                           float h, float cull, float* f) {
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float d2 = dist2(rx, ry, rz);
     const float rsq = d2 > 0.f ? rsqrtf(d2) : 0.f;  // coincident pair (or self): r = 0, no push
@@ -621,13 +630,33 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
     f[3] = fmaf(vj.x - vi.x, wv, f[3]);
     f[4] = fmaf(vj.y - vi.y, wv, f[4]);
     f[5] = fmaf(vj.z - vi.z, wv, f[5]);
+    if (FEAT) {
+        const float ux = vi.x - vj.x, uy = vi.y - vj.y, uz = vi.z - vj.z;
+        const float ru = fmaf(rz, uz, fmaf(ry, uy, rx * ux));
+        const float dp = ru * rsq;  // d'
+        if (pres > 0.f) {
+            const float coef = pres * hd * hd * rsq;
+            const float dcoef = -pres * hd * rsq * (2.f + hd * rsq);  // d coef / d d
+            const float cr = dcoef * dp;
+            f[6] = fmaf(cr, rx, fmaf(coef, ux, f[6]));
+            f[7] = fmaf(cr, ry, fmaf(coef, uy, f[7]));
+            f[8] = fmaf(cr, rz, fmaf(coef, uz, f[8]));
+        }
+        const float wj = dp * inv_rho;
+        f[9] = fmaf(ux, wj, f[9]);
+        f[10] = fmaf(uy, wj, f[10]);
+        f[11] = fmaf(uz, wj, f[11]);
+        const float w = fmaxf(cull - d2, 0.f);
+        f[12] = fmaf(w * w, ru, f[12]);
+    }
 }
 
 // A lane's list (entries list[e * 32 + lane], e < cnt), four entries per round so their loads
 // overlap; an empty place takes the particle itself (slot self), whose terms are exactly zero.
+template <bool FEAT>
 __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t cnt, uint32_t lane, uint32_t self,
                                                 const float4& pi, const float4& vi, const float4* __restrict__ pos,
-                                                const float4* __restrict__ vel, float h, float f[6]) {
+                                                const float4* __restrict__ vel, float h, float cull, float* f) {
     for (uint32_t e = 0; e < cnt; e += 4u) {
         uint32_t k[4];
 #pragma unroll
@@ -639,17 +668,18 @@ __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t c
             vj[u] = __ldg(vel + k[u]);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) pair_terms(pi, vi, pj[u], vj[u], h, f);
+        for (int u = 0; u < 4; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], h, cull, f);
     }
 }
 
 // Gravity, reference-only external terms, symplectic Euler, speed clamp and wall collision
 // (update.comp:145,191-231), then the store into the state buffer.
+template <bool FEAT>
 __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const StepInputs& in, const float4& pi,
-                                                const float4& vi, const float f[6], uint32_t ti,
+                                                const float4& vi, const float* f, uint32_t ti,
                                                 float4* __restrict__ pos_a, float4* __restrict__ vel_a,
                                                 const uint32_t* __restrict__ ids_b, uint32_t* __restrict__ ids_a,
-                                               float4* __restrict__ accel) {
+                                                float4* __restrict__ accel, float4* __restrict__ feat) {
     const float fp_scale = -sc.m * sc.cs;         // -m * spiky const
     const float fv_scale = sc.m * sc.cv * sc.mu;  // m * visc const * mu
     const float rho = pi.w, pressure = vi.w;
@@ -692,10 +722,19 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     vel_a[ti] = make_float4(v[0], v[1], v[2], pressure);
     if (ids_a) ids_a[ti] = ids_b[ti];
     if (accel) accel[ti] = make_float4(acc[0], acc[1], acc[2], 0.f);
+    if (FEAT) {
+        // d a / dt under the neighbours' relative motion (pressures and densities held), and the
+        // density rate of the Poly6 sum
+        float jk[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) jk[a] = (fp_scale * f[6 + a] + fv_scale * f[9 + a]) * inv;
+        feat[ti] = make_float4(jk[0], jk[1], jk[2], -6.f * sc.m * sc.c6 * f[12]);
+    }
 }
 
-template <bool BATCHED>
-__global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts sc0, const BatchTables bt,
+// FEAT: the learned rollout's judge step; also writes feat[] (d a/dt, density rate), see pair_terms.
+template <bool BATCHED, bool FEAT = false>
+__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) force_kernel(const SceneConsts sc0, const BatchTables bt,
                                                                const StepInputs in, const uint32_t n,
                                                                const uint32_t num_cells,
                                                                const float4* __restrict__ pos_b,
@@ -708,7 +747,9 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                                                                uint32_t* __restrict__ num_nonempty,  // [0] cells, [1]/[2] counters
                                                                const uint32_t* __restrict__ hits,
                                                                float4* __restrict__ accel,
-                                                               uint32_t* __restrict__ err) {
+                                                               uint32_t* __restrict__ err,
+                                                               float4* __restrict__ feat = nullptr) {
+    constexpr int NF = FEAT ? NF_FEAT : NF_PLAIN;
     // Per warp: the slot table (candidate number -> sorted slot), then the dense path's per-lane
     // lists and its x/y/z stage; the replay path's neighbour lists use both of those regions.
     __shared__ __align__(16) uint32_t s_work[WARPS][STAGE_CAP + FORCE_REPLAY_LIST];
@@ -773,7 +814,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
             const uint32_t ti = cr.cbeg + tm.t;
             const float4 pi = pos_b[ti];
             const float4 vi = vel_b[ti];
-            float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float f[NF] = {};
             // Each lane's hit count, its offset among its target's slices, the target's total,
             // and the target's segment in the warp's neighbour list (targets in order).
             uint32_t cnt = 0;
@@ -836,7 +877,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                             vj[u] = __ldg(vel_b + k[u]);
                         }
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) pair_terms(pi, vi, pj[u], vj[u], sc.h, f);
+                        for (int u = 0; u < 4; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], sc.h, sc.cull, f);
                     }
                 }
             } else if (tm.active) {
@@ -870,13 +911,13 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                             vj[u] = __ldg(vel_b + k[u]);
                         }
 #pragma unroll
-                        for (int u = 0; u < 2; ++u) pair_terms(pi, vi, pj[u], vj[u], sc.h, f);
+                        for (int u = 0; u < 2; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], sc.h, sc.cull, f);
                     }
                 }
             }
 #pragma unroll
-            for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
-            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
+            for (int q = 0; q < NF; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
+            if (tm.sl == 0u) integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, feat);
             __syncwarp();  // the slot table is rewritten for the next cell
             continue;
         }
@@ -893,7 +934,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
             const uint32_t ti = t0 + tm.t;
             const float4 pi = pos_b[ti];
             const float4 vi = vel_b[ti];
-            float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float f[NF] = {};
             uint32_t cnt = 0;
             if (hits != nullptr && bits_fit(cr.total, tm.S)) {
                 const uint32_t IT = (((cr.total + 3u) >> 2) + tm.S - 1u) / tm.S;
@@ -920,7 +961,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                                 list[(cnt++) * 32u + lane] = q < len ? slot[q] : ti;
                             }
                             if (!__any_sync(FULL, word != 0u)) break;
-                            accumulate_list(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, f);
+                            accumulate_list<FEAT>(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, sc.cull, f);
                             cnt = 0;
                         }
                     }
@@ -942,7 +983,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                     const ulonglong2* qx = reinterpret_cast<const ulonglong2*>(fx) + rsl;
                     for (uint32_t j = 0; j < IT; ++j, qx += tm.S) {
                         if (__any_sync(FULL, cnt + 4u > (uint32_t)FORCE_LIST_CAP)) {
-                            accumulate_list(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, f);
+                            accumulate_list<FEAT>(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, sc.cull, f);
                             cnt = 0;
                         }
                         uint32_t bits = quad_test<FORCE_STAGE>(qx, px, py, pz, cull2);
@@ -959,40 +1000,222 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                     }
                 }
             }
-            accumulate_list(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, f);
+            accumulate_list<FEAT>(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, sc.cull, f);
 #pragma unroll
-            for (int q = 0; q < 6; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
-            if (tm.sl == 0u) integrate_store(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
+            for (int q = 0; q < NF; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
+            if (tm.sl == 0u) integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, feat);
         }
         __syncwarp();  // the slot table and stage are rewritten for the next cell
     }
     release_counter(counter, m, M, lane);
 }
 
+// ---- force + integration, one lane per target ------------------------------------------------
+//
+// A warp takes 32 consecutive sorted slots (dynamic scheduling over chunks of 32) and each lane
+// owns one target. The lane recomputes its cell from its position (the sort's binning), the 9
+// row ranges of the cell's 27 neighbour cells in the density pass's candidate numbering, and the
+// density pass's team split of the target's chunk of the cell (its slice count S), and decodes
+// the target's bit strings (word w of slice s holds quads s + (8 w + j) S, j = 0..7) into a
+// per-lane list of neighbour slots; the list is evaluated four neighbours per round whenever it
+// fills. Targets whose bit strings the density pass did not keep test their candidates directly.
+
+constexpr uint32_t LANE_LIST = 32;  // neighbour slots a lane collects before evaluating them
+
+// The row of candidate q (the last row whose first candidate is <= q) and its slot, from the row
+// starts P[0..8] (P[0] = 0, non-decreasing) and offsets D[r] = first slot of row r - P[r].
+__device__ __forceinline__ uint32_t slot_of(uint32_t q, const uint32_t P[9], const uint32_t D[9]) {
+    const bool b4 = q >= P[4];
+    const bool b2 = q >= (b4 ? P[6] : P[2]);
+    const bool b1 = q >= (b4 ? (b2 ? P[7] : P[5]) : (b2 ? P[3] : P[1]));
+    uint32_t d = b4 ? (b2 ? (b1 ? D[7] : D[6]) : (b1 ? D[5] : D[4])) : (b2 ? (b1 ? D[3] : D[2]) : (b1 ? D[1] : D[0]));
+    if (b4 && b2 && b1 && q >= P[8]) d = D[8];
+    return q + d;
+}
+
+template <bool BATCHED, bool FEAT = false>
+__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 2 : 3) force_lane_kernel(
+    const SceneConsts sc0, const BatchTables bt, const StepInputs in, const uint32_t n, const uint32_t num_cells,
+    const float4* __restrict__ pos_b, const float4* __restrict__ vel_b, const uint32_t* __restrict__ ids_b,
+    float4* __restrict__ pos_a, float4* __restrict__ vel_a, uint32_t* __restrict__ ids_a,
+    const uint32_t* __restrict__ start, const uint32_t* __restrict__ cell_list,
+    uint32_t* __restrict__ num_nonempty,  // [2]: this pass's chunk counter
+    const uint32_t* __restrict__ hits, float4* __restrict__ accel, uint32_t* __restrict__ err,
+    float4* __restrict__ feat = nullptr) {
+    constexpr int NF = FEAT ? NF_FEAT : NF_PLAIN;
+    __shared__ uint32_t s_list[WARPS][LANE_LIST * 32];
+    __shared__ uint32_t s_poff[BATCHED ? MAX_SCENES + 1 : 1];
+    __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
+    if (BATCHED) {
+        for (uint32_t t = threadIdx.x; t <= bt.num_scenes; t += blockDim.x) {
+            s_poff[t] = bt.poff[t];
+            s_coff[t] = bt.coff[t];
+        }
+        __syncthreads();
+    }
+    (void)cell_list;
+    (void)num_cells;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t* list = s_list[threadIdx.x >> 5];
+    const uint32_t M = (n + 31u) >> 5;  // chunks of 32 slots
+    uint32_t* const counter = num_nonempty + 2;
+    uint32_t m_next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
+    uint32_t m = __shfl_sync(FULL, m_next, 0);
+    for (; m < M; m = __shfl_sync(FULL, m_next, 0)) {
+        if (lane == 0) m_next = atomicAdd(counter, 1u);
+        const uint32_t ti = (m << 5) + lane;
+        const bool live = ti < n;
+        const uint32_t tself = live ? ti : n - 1u;
+        SceneConsts sc;
+        uint32_t coff = 0;
+        if (BATCHED) {
+            const uint32_t s = find_scene(s_poff, bt.num_scenes, tself);
+            sc = bt.scenes[s];
+            coff = s_coff[s];
+        } else {
+            sc = sc0;
+        }
+        const uint32_t* tab = start + coff;
+        const float4 pi = pos_b[tself];
+        const float4 vi = vel_b[tself];
+        int32_t cx, cy, cz;
+        const uint32_t c = bin_key(pi.x, pi.y, pi.z, sc.bin, sc.R, &cx, &cy, &cz);
+        const uint32_t cend = min(__ldg(tab + c + 1), n);
+        const uint32_t cbeg = min(__ldg(tab + c), cend);
+        const uint32_t ncell = cend - cbeg;
+        // rows of the 27 neighbour cells, in the density pass's candidate numbering
+        uint32_t P[9], D[9], total = 0;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int yy = cy + (r % 3) - 1, zz = cz + (r / 3) - 1;
+            uint32_t lo = 0, hi = 0;
+            if (yy >= 0 && yy < sc.R && zz >= 0 && zz < sc.R) {
+                const int x0 = cx > 0 ? cx - 1 : 0;
+                const int x1 = cx + 1 < sc.R ? cx + 1 : sc.R - 1;
+                const uint32_t row = (uint32_t)((zz * sc.R + yy) * sc.R);
+                hi = min(__ldg(tab + row + x1 + 1), n);
+                lo = min(__ldg(tab + row + x0), hi);
+            }
+            P[r] = total;
+            D[r] = lo - total;
+            total += hi - lo;
+        }
+        const bool overfull = ncell > MAX_CELL_PARTICLES;
+        // the density pass's team for this target's chunk of the cell
+        const uint32_t inchunk = live && !overfull && ti >= cbeg && ti < cend;
+        const uint32_t t0 = cbeg + ((tself - cbeg) & ~31u);
+        const uint32_t nt = inchunk ? min(32u, cend - t0) : 1u;
+        const uint32_t S = (uint32_t)(32.5f * __frcp_rn((float)nt));
+        const bool single = ncell <= 32u;
+        const bool kept = hits != nullptr && (bits_fit(total, S) || mask_shape(total, S, single).ok);
+        const uint32_t IT = (((total + 3u) >> 2) + S - 1u) / S;
+        const uint32_t nwords = (IT + 7u) >> 3;
+        float f[NF] = {};
+        // candidate generator state: bit strings (w, s, word) or direct tests (q)
+        bool more = inchunk && total > 0;
+        uint32_t w = 0, sl = 0, word = 0, q = 0;
+        if (more && kept) word = __ldg(hits + (size_t)ti * MASK_WORDS);
+        for (;;) {
+            uint32_t cnt = 0;
+            while (more && cnt < LANE_LIST) {
+                if (kept) {
+                    if (word == 0u) {
+                        if (++sl == S) {
+                            sl = 0;
+                            ++w;
+                        }
+                        if (w >= nwords) {
+                            more = false;
+                            break;
+                        }
+                        word = __ldg(hits + (size_t)ti * MASK_WORDS + w * S + sl);
+                        continue;
+                    }
+                    const uint32_t b = (uint32_t)__ffs(word) - 1u;
+                    word &= word - 1u;
+                    const uint32_t cq = 4u * (sl + (8u * w + (b >> 2)) * S) + (b & 3u);
+                    // bits always come from this step's density pass over the same tables; the
+                    // check only keeps a stage-by-stage caller's stale bits in bounds
+                    if (cq < total) {
+                        const uint32_t k = slot_of(cq, P, D);
+                        list[cnt * 32u + lane] = k < n ? k : ti;
+                        ++cnt;
+                    }
+                } else {
+                    if (q >= total) {
+                        more = false;
+                        break;
+                    }
+                    const uint32_t k = min(slot_of(q, P, D), n - 1u);
+                    ++q;
+                    const float4 pj = __ldg(pos_b + k);
+                    const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+                    if (d2 <= sc.cull) list[(cnt++) * 32u + lane] = k;  // the target itself adds zero
+                }
+            }
+            if (!__any_sync(FULL, cnt > 0u)) break;
+            accumulate_list<FEAT>(list, cnt, lane, tself, pi, vi, pos_b, vel_b, sc.h, sc.cull, f);
+            if (!__any_sync(FULL, more)) break;
+        }
+        if (live) {
+            if (overfull) {
+                // not evaluated (see MAX_CELL_PARTICLES): the particle keeps its state, reported
+                pos_a[ti] = pi;
+                vel_a[ti] = vi;
+                if (ids_a) ids_a[ti] = ids_b[ti];
+                if (accel) accel[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (FEAT) feat[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (ti == cbeg && err) atomicOr(err, DEVERR_CELL_OVERFLOW);
+            } else {
+                integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, feat);
+            }
+        }
+    }
+    // the chunk counter returns to zero for the next launch (see release_counter)
+    if (lane == 0 && m == M + gridDim.x * (uint32_t)WARPS - 1u) atomicExch(counter, 0u);
+}
+
+template <class... A>
+constexpr int arity(void (*)(A...)) {
+    return (int)sizeof...(A);
+}
+// A captured step's force node is re-parameterised from ForceKernelArgs: one pointer per
+// kernel parameter.
+static_assert(arity(&force_kernel<false, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
+static_assert(arity(&force_lane_kernel<false, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
+static_assert(arity(&force_lane_kernel<true, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
+
 }  // namespace
 
-void sph_occupancy(bool batched, int* density_blocks, int* force_blocks) {
+void sph_occupancy(bool batched, int* density_blocks, int* force_blocks, int force_variant) {
     int bd = 0, bf = 0;
     if (batched) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<true>, SPH_THREADS, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<true>, SPH_THREADS, 0);
+        if (force_variant == FORCE_LANE)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_lane_kernel<true>, SPH_THREADS, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<true>, SPH_THREADS, 0);
     } else {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<false>, SPH_THREADS, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<false>, SPH_THREADS, 0);
+        if (force_variant == FORCE_LANE)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_lane_kernel<false>, SPH_THREADS, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<false>, SPH_THREADS, 0);
     }
     *density_blocks = bd > 0 ? bd : 1;
     *force_blocks = bf > 0 ? bf : 1;
 }
 
-LaunchDims compute_launch_dims(int device) {
+LaunchDims compute_launch_dims(int device, int force_variant) {
     LaunchDims ld;
     cudaDeviceGetAttribute(&ld.sms, cudaDevAttrMultiProcessorCount, device);
     if (ld.sms <= 0) ld.sms = 1;
     int bd = 1, bf = 1;
-    sph_occupancy(false, &bd, &bf);
+    sph_occupancy(false, &bd, &bf, force_variant);
     ld.grid_density = ld.sms * bd;
     ld.grid_force = ld.sms * bf;
     ld.grid_stream = ld.sms * 8;
+    ld.force_variant = force_variant;
     return ld;
 }
 
@@ -1003,27 +1226,70 @@ void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims
         (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr, d.hits, d.err);
 }
 
-void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
-                  cudaStream_t s) {
-    force_kernel<false><<<ld.grid_force, SPH_THREADS, 0, s>>>(sc, BatchTables{}, in, d.n, d.num_cells, d.pos_b,
-                                                              d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
-                                                              d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
-}
-
 void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
     density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
         SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
         reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
 }
 
-void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
-                          cudaStream_t s) {
-    force_kernel<true><<<ld.grid_force, SPH_THREADS, 0, s>>>(SceneConsts{}, bt, in, d.n, d.num_cells, d.pos_b,
-                                                             d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
-                                                             d.cell_list, d.num_nonempty, d.hits, d.accel, d.err);
+// The force pass of variant `ld.force_variant` (FEAT: the judge steps' feature output too), on a
+// persistent grid sized from that kernel's occupancy.
+template <bool BATCHED, bool FEAT>
+void launch_force_any(const DevBuffers& d, const SceneConsts& sc, const BatchTables& bt, const StepInputs& in,
+                      const LaunchDims& ld, float4* feat, cudaStream_t s) {
+    const bool lane = ld.force_variant == FORCE_LANE;
+    int grid = ld.grid_force;
+    if (FEAT) {
+        // more registers per thread than the plain kernel: its own occupancy (cached per variant)
+        static int blocks[2] = {0, 0};
+        int& b = blocks[lane ? 1 : 0];
+        if (!b) {
+            if (lane)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, force_lane_kernel<BATCHED, true>, SPH_THREADS, 0);
+            else
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, force_kernel<BATCHED, true>, SPH_THREADS, 0);
+            if (b <= 0) b = 1;
+        }
+        grid = ld.sms * b;
+    }
+    if (lane)
+        force_lane_kernel<BATCHED, FEAT><<<grid, SPH_THREADS, 0, s>>>(
+            sc, bt, in, d.n, d.num_cells, d.pos_b, d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start, d.cell_list,
+            d.num_nonempty, d.hits, d.accel, d.err, feat);
+    else
+        force_kernel<BATCHED, FEAT><<<grid, SPH_THREADS, 0, s>>>(sc, bt, in, d.n, d.num_cells, d.pos_b, d.vel_b,
+                                                                d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
+                                                                d.cell_list, d.num_nonempty, d.hits, d.accel, d.err,
+                                                                feat);
 }
 
-const void* force_kernel_symbol(uint32_t) { return reinterpret_cast<const void*>(&force_kernel<false>); }
-const void* force_kernel_batched_symbol() { return reinterpret_cast<const void*>(&force_kernel<true>); }
+void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
+                  cudaStream_t s) {
+    launch_force_any<false, false>(d, sc, BatchTables{}, in, ld, nullptr, s);
+}
+
+void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
+                          cudaStream_t s) {
+    launch_force_any<true, false>(d, SceneConsts{}, bt, in, ld, nullptr, s);
+}
+
+void launch_force_feat(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
+                       float4* feat, cudaStream_t s) {
+    launch_force_any<false, true>(d, sc, BatchTables{}, in, ld, feat, s);
+}
+
+void launch_force_batched_feat(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
+                               float4* feat, cudaStream_t s) {
+    launch_force_any<true, true>(d, SceneConsts{}, bt, in, ld, feat, s);
+}
+
+const void* force_kernel_symbol(int force_variant) {
+    return force_variant == FORCE_LANE ? reinterpret_cast<const void*>(&force_lane_kernel<false>)
+                                       : reinterpret_cast<const void*>(&force_kernel<false>);
+}
+const void* force_kernel_batched_symbol(int force_variant) {
+    return force_variant == FORCE_LANE ? reinterpret_cast<const void*>(&force_lane_kernel<true>)
+                                       : reinterpret_cast<const void*>(&force_kernel<true>);
+}
 
 }  // namespace wc

@@ -628,7 +628,9 @@ __global__ void fluid_diag_kernel(uint32_t n, const float4* __restrict__ pos, co
         for (int q = 0; q < 5; ++q) part[(size_t)blockIdx.x * 5 + q] = sacc[q][0];
 }
 
-wc_status fluid_diag(wc_fluid* f, double out[6]) {
+}  // namespace
+
+wc_status wc::fluid_diagnostics(wc_fluid* f, double out[6]) {
     FluidInternals fi = fluid_internals(f);
     const uint32_t blocks = 256;
     double* part = nullptr;
@@ -647,6 +649,8 @@ wc_status fluid_diag(wc_fluid* f, double out[6]) {
     }
     return WC_OK;
 }
+
+namespace {
 
 // history (state order) <- [v_new, gathered history shifted by one] (sorted order of this step)
 __global__ void shift_history_kernel(uint32_t n, const float4* __restrict__ vel, const float4* __restrict__ hs,
@@ -1061,7 +1065,7 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
         // plain SPH: the graph-launched solver, timed like the other modes
         FluidInternals fi = fluid_internals(f);
         WC_CUDA_TRY(cudaStreamSynchronize(fi.stream));
-        WC_TRY(fluid_diag(f, out->diag_start));
+        WC_TRY(fluid_diagnostics(f, out->diag_start));
         cudaEvent_t e0, e1;
         WC_CUDA_TRY(cudaEventCreate(&e0));
         WC_CUDA_TRY(cudaEventCreate(&e1));
@@ -1085,7 +1089,7 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
         out->ms_device = ms;
         out->ms_wall = std::chrono::duration<double, std::milli>(t1 - t0).count();
         out->particle_steps_per_s = ms > 0 ? (double)fi.d->n * nsteps / (ms * 1e-3) : 0.0;
-        return fluid_diag(f, out->diag_end);
+        return fluid_diagnostics(f, out->diag_end);
     }
     FluidInternals fi = fluid_internals(f);
     const uint32_t n = fi.d->n;
@@ -1112,7 +1116,7 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
     const bool needs_accel = mode == WC_ROLLOUT_STALE || mode == WC_ROLLOUT_HYBRID;
     if (needs_accel && !was_recording) WC_TRY(wc_fluid_set_recording(f, 1));
     WC_CUDA_TRY(cudaStreamSynchronize(fi.stream));
-    WC_TRY(fluid_diag(f, out->diag_start));
+    WC_TRY(fluid_diagnostics(f, out->diag_start));
     cudaStream_t own = s->stream;
     s->stream = fi.stream;  // everything runs on the fluid's stream
     s->dt = dt;
@@ -1123,7 +1127,7 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
     if (needs_accel && !was_recording) wc_fluid_set_recording(f, 0);
     if (rc != WC_OK) return rc;
     WC_TRY(read_err(s));
-    return fluid_diag(f, out->diag_end);
+    return fluid_diagnostics(f, out->diag_end);
 }
 
 }  // extern "C"

@@ -1,0 +1,149 @@
+"""The learned fast rollout over the C ABI (wc_local_*): a per-particle network on the sums of
+the judge step's SPH passes predicts the accelerations of the next K - 1 steps, which then run
+without neighbour passes; every K-th step is plain SPH and judges the last cycle by the carried
+density. No counterpart in the reference, which only runs plain SPH.
+
+The network, its fused tensor-core inference, training and the rollout are in
+csrc/wc_local.cu; this module moves host arrays and drives training.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi as A
+from ._abi import LocalConfig, RolloutStats, check, lib
+from .batch import Batch
+from .fluid import Fluid
+
+IN, HIDDEN, OUT = 32, 64, 16
+INPUT_NAMES = ["a_x", "a_y", "a_z", "jdt_x", "jdt_y", "jdt_z", "rhodot", "v_x", "v_y", "v_z", "rho_rel", "p_rel",
+               "wall_x0", "wall_x1", "wall_y0", "wall_y1", "wall_z0", "wall_z1", "k_rel"]
+DEFAULT_WEIGHTS = Path(__file__).resolve().parent / "weights" / "local_k4.npz"
+
+
+def default_config(**overrides) -> LocalConfig:
+    c = LocalConfig()
+    lib().wc_local_config_default(C.byref(c))
+    for k, v in overrides.items():
+        setattr(c, k, v)
+    return c
+
+
+class LocalNet:
+    """One per-particle network: FP32 master weights, Adam state, sample sets and scratch."""
+
+    def __init__(self, config: LocalConfig | None = None, **overrides):
+        cfg = config if config is not None else default_config(**overrides)
+        h = C.c_void_p()
+        check(lib().wc_local_create(C.byref(cfg), C.byref(h)), "wc_local_create")
+        self._h = h
+        self.config = cfg
+        self.ages = int(cfg.ages)
+        self.num_params = int(lib().wc_local_num_params(h))
+
+    # ---- parameters ---------------------------------------------------------------------------
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(lib().wc_local_get_params(self._h, A._ptr(out), self.num_params), "wc_local_get_params")
+        return out
+
+    def set_params(self, w: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        check(lib().wc_local_set_params(self._h, A._ptr(w), w.size), "wc_local_set_params")
+
+    # ---- samples and training -------------------------------------------------------------------
+    def record(self, target, dt: float, cycles: int, held_out: bool = False) -> None:
+        if isinstance(target, Batch):
+            check(lib().wc_local_record_batch(self._h, target._h, float(dt), int(cycles), int(held_out)),
+                  "wc_local_record_batch")
+        else:
+            check(lib().wc_local_record_fluid(self._h, target._require(), float(dt), int(cycles), int(held_out)),
+                  "wc_local_record_fluid")
+
+    def num_samples(self, held_out: bool = False) -> int:
+        return int(lib().wc_local_num_samples(self._h, int(held_out)))
+
+    def clear_samples(self) -> None:
+        check(lib().wc_local_clear_samples(self._h), "wc_local_clear_samples")
+
+    def samples(self, held_out: bool = False, first: int = 0, count: int | None = None):
+        if count is None:
+            count = self.num_samples(held_out) - first
+        x = np.zeros((count, IN), np.float32)
+        y = np.zeros((count, OUT), np.float32)
+        check(lib().wc_local_get_samples(self._h, int(held_out), first, count, A._ptr(x), A._ptr(y)),
+              "wc_local_get_samples")
+        return x, y
+
+    def train(self, steps: int, rows: int = 8192, lr: float = 1e-3) -> np.ndarray:
+        loss = np.zeros(steps, np.float32)
+        check(lib().wc_local_train(self._h, int(steps), int(rows), float(lr), A._ptr(loss)), "wc_local_train")
+        return loss
+
+    def gradients(self, rows_idx: np.ndarray):
+        idx = np.ascontiguousarray(rows_idx, dtype=np.uint32)
+        g = np.zeros(self.num_params, np.float32)
+        loss = np.zeros(1, np.float32)
+        check(lib().wc_local_gradients(self._h, A._ptr(idx), idx.size, A._ptr(g), A._ptr(loss)), "wc_local_gradients")
+        return g, float(loss[0])
+
+    def evaluate(self, held_out: bool = True):
+        """(network error, stale error) per age: relative L2 of the acceleration."""
+        a = np.zeros(self.ages, np.float32)
+        b = np.zeros(self.ages, np.float32)
+        check(lib().wc_local_evaluate(self._h, int(held_out), A._ptr(a), A._ptr(b)), "wc_local_evaluate")
+        return a, b
+
+    def predict(self, fluid: Fluid, dt: float):
+        """(inputs [n, 32], acceleration changes [n, 3 ages]) of the fluid's current state, in the
+        order of the judge step's sort; the fluid does not advance."""
+        n = fluid.numParticles()
+        x = np.zeros((n, IN), np.float32)
+        y = np.zeros((n, 3 * self.ages), np.float32)
+        check(lib().wc_local_predict(self._h, fluid._require(), float(dt), A._ptr(x), A._ptr(y)), "wc_local_predict")
+        return x, y
+
+    def close(self) -> None:
+        if self._h is not None:
+            lib().wc_local_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def rollout(fluid: Fluid, dt: float, nsteps: int, ages: int = 3, tolerance: float = 0.01,
+            net: LocalNet | None = None) -> dict:
+    """Cycles of one judge SPH step and `ages` steps on predicted accelerations (net None: the
+    stale SPH acceleration, the method without the network)."""
+    st = RolloutStats()
+    h = net._h if net is not None else None
+    check(lib().wc_local_rollout(h, fluid._require(), float(dt), int(nsteps), int(ages), float(tolerance),
+                                 C.byref(st)), "wc_local_rollout")
+    return st.as_dict()
+
+
+def save_weights(net: LocalNet, path: Path = DEFAULT_WEIGHTS, **meta) -> None:
+    path.parent.mkdir(parents=True, exist_ok=True)
+    np.savez(path, params=net.params(), ages=np.int32(net.ages), accel_scale=np.float32(net.config.accel_scale),
+             velocity_scale=np.float32(net.config.velocity_scale), **meta)
+
+
+def load_weights(path: Path = DEFAULT_WEIGHTS, **overrides) -> LocalNet:
+    z = np.load(path)
+    net = LocalNet(ages=int(z["ages"]), accel_scale=float(z["accel_scale"]), velocity_scale=float(z["velocity_scale"]),
+                   **overrides)
+    net.set_params(z["params"])
+    return net
