@@ -76,10 +76,10 @@ enum {
        replacement for its pseudo wall density and force that its report names as the next
        physics fix. */
     WC_FLAG_WALL_WEIGHTS = 1u << 6,
-    /* Run the force pass as one 32-lane team per non-empty cell (WC_FORCE_TEAM) instead of one
-       lane per target (the default, WC_FORCE_LANE); the same neighbour sets, the sums differ
-       only in the order of their additions. */
-    WC_FLAG_FORCE_TEAM = 1u << 7
+    /* Run both neighbour passes (density, force) as one 32-lane team per non-empty cell
+       (WC_PASSES_TEAM) instead of one lane per target (the default, WC_PASSES_LANE); the same
+       neighbour sets, the sums differ only in the order of their additions. */
+    WC_FLAG_CELL_TEAMS = 1u << 7
 };
 
 /* The reference's four active behaviours. */
@@ -317,10 +317,11 @@ WC_API void wc_batch_destroy(wc_batch* b);
 
 /* Launch geometry the autotuner picks: resident blocks per SM of the two neighbour passes and
    of the per-particle kernels, and the cell edge as a multiple of each scene's h. */
-/* Force pass variants (threads per cell): one 32-lane team per non-empty cell, its targets split
-   into slices, or one lane per target. Same neighbour sets; sums differ in addition order only. */
-#define WC_FORCE_TEAM 0
-#define WC_FORCE_LANE 1
+/* Neighbour pass variants (threads per cell): one 32-lane team per non-empty cell, its targets
+   split into slices, or one lane per target. Same neighbour sets; sums differ in addition order
+   only. */
+#define WC_PASSES_TEAM 0
+#define WC_PASSES_LANE 1
 
 typedef struct wc_tuning {
     uint32_t density_blocks_per_sm;
@@ -329,7 +330,7 @@ typedef struct wc_tuning {
     float cell_factor;
     float step_ms; /* best measured step time */
     uint32_t trials;
-    uint32_t force_variant; /* WC_FORCE_TEAM or WC_FORCE_LANE */
+    uint32_t pass_variant; /* WC_PASSES_TEAM or WC_PASSES_LANE */
 } wc_tuning;
 
 /* Time graph replays of candidate geometries (the state is saved before and restored after,

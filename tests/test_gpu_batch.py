@@ -68,7 +68,7 @@ def test_tuner_keeps_state_and_picks_valid_geometry(gpu):
         assert b.particles().tobytes() == before.tobytes()
         assert t.trials >= 5 and t.step_ms > 0
         assert t.density_blocks_per_sm >= 1 and t.force_blocks_per_sm >= 1 and t.cell_factor in (1.0, 1.25)
-        assert t.force_variant in (_abi.WC_FORCE_TEAM, _abi.WC_FORCE_LANE)
+        assert t.pass_variant in (_abi.WC_PASSES_TEAM, _abi.WC_PASSES_LANE)
         m0 = b.diagnostics()[:, 0].copy()
         b.step(1e-3, 3)
         after = b.particles()

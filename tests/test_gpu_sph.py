@@ -46,9 +46,13 @@ def eos_tolerance(p, rho64):
     return DENSITY_RTOL * 3.0 * k * np.abs(x) ** 3 + 1e-6
 
 
+@pytest.mark.parametrize("variant", ["lane", "team"])
 @pytest.mark.parametrize("name,steps,dt", CASES)
-def test_density_pressure_neighbours(gpu, oracle, name, steps, dt):
+def test_density_pressure_neighbours(gpu, oracle, name, steps, dt, variant):
+    """Both pass variants: one lane per target (the default) and a 32-lane team per cell."""
     p, st = evolved(name, steps, dt, _abi.WC_FLAG_NEIGHBOR_COUNTS)
+    if variant == "team":
+        p.flags |= _abi.WC_FLAG_CELL_TEAMS
     srt, nc, perm = gpu_density(p, st)
     o_sorted, _, o_perm, counts, offsets = oracle.sort(p, st)
     assert np.array_equal(perm, o_perm)
@@ -74,10 +78,10 @@ def test_density_pressure_neighbours(gpu, oracle, name, steps, dt):
 @pytest.mark.parametrize("variant", ["lane", "team"])
 @pytest.mark.parametrize("name,steps,dt", CASES)
 def test_force_integration_pass(gpu, oracle, name, steps, dt, variant):
-    """Both force pass variants: one lane per target (the default) and a 32-lane team per cell."""
+    """Both pass variants: one lane per target (the default) and a 32-lane team per cell."""
     p, st = evolved(name, steps, dt)
     if variant == "team":
-        p.flags |= _abi.WC_FLAG_FORCE_TEAM
+        p.flags |= _abi.WC_FLAG_CELL_TEAMS
     with fluid(p, st) as f:
         f.sort()
         f.density()
@@ -213,12 +217,12 @@ def test_wall_weights_keep_particles_off_the_walls(gpu):
     assert frac[_abi.WC_FLAG_WALL_WEIGHTS] < 0.85 * frac[0], frac
 
 
-def test_force_variants_agree(gpu):
+def test_pass_variants_agree(gpu):
     """The two force pass variants evaluate the same neighbour sets; over 50 steps of the 16,384
     particle dam break their trajectories differ only by rounding (the order of the sums)."""
     p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
     q = p.copy()
-    q.flags |= _abi.WC_FLAG_FORCE_TEAM
+    q.flags |= _abi.WC_FLAG_CELL_TEAMS
     out = []
     for prm in (p, q):
         with fluid(prm, st) as f:

@@ -35,9 +35,9 @@ WC_FLAG_MOUSE_FORCE = 1 << 3
 WC_FLAG_TRACK_IDS = 1 << 4
 WC_FLAG_NEIGHBOR_COUNTS = 1 << 5
 WC_FLAG_WALL_WEIGHTS = 1 << 6
-WC_FLAG_FORCE_TEAM = 1 << 7
-WC_FORCE_TEAM = 0
-WC_FORCE_LANE = 1
+WC_FLAG_CELL_TEAMS = 1 << 7
+WC_PASSES_TEAM = 0
+WC_PASSES_LANE = 1
 WC_FLAGS_REFERENCE = WC_FLAG_WALL_DENSITY | WC_FLAG_WALL_FORCE | WC_FLAG_SPEED_CLAMP | WC_FLAG_MOUSE_FORCE
 
 WC_BUFFER_STATE = 1
@@ -137,7 +137,7 @@ class Tuning(C.Structure):
         ("cell_factor", C.c_float),
         ("step_ms", C.c_float),
         ("trials", C.c_uint32),
-        ("force_variant", C.c_uint32),
+        ("pass_variant", C.c_uint32),
     ]
 
 

@@ -190,12 +190,12 @@ wc_status apply_cell_factor(wc_batch* b, float factor) {
 }
 
 void apply_geometry(wc_batch* b, const wc_tuning& t) {
-    const int variant = t.force_variant == WC_FORCE_TEAM ? FORCE_TEAM : FORCE_LANE;
-    if (variant != b->ld.force_variant) {
-        b->ld.force_variant = variant;
+    const int variant = t.pass_variant == WC_PASSES_TEAM ? PASSES_TEAM : PASSES_LANE;
+    if (variant != b->ld.pass_variant) {
+        b->ld.pass_variant = variant;
         sph_occupancy(true, &b->max_density_blocks, &b->max_force_blocks, variant);
     }
-    b->tuning.force_variant = (uint32_t)variant;
+    b->tuning.pass_variant = (uint32_t)variant;
     b->ld.grid_density = b->ld.sms * (int)std::max(1u, std::min(t.density_blocks_per_sm, (uint32_t)b->max_density_blocks));
     b->ld.grid_force = b->ld.sms * (int)std::max(1u, std::min(t.force_blocks_per_sm, (uint32_t)b->max_force_blocks));
     b->ld.grid_stream = b->ld.sms * (int)std::max(1u, t.stream_blocks_per_sm);
@@ -233,7 +233,7 @@ wc_status capture(wc_batch* b, const StepInputs& in) {
         if (ty != cudaGraphNodeTypeKernel) continue;
         cudaKernelNodeParams kp;
         WC_CUDA_TRY(cudaGraphKernelNodeGetParams(nd, &kp));
-        if (kp.func == force_kernel_batched_symbol(b->ld.force_variant)) {
+        if (kp.func == force_kernel_batched_symbol(b->ld.pass_variant)) {
             b->force_node = nd;
             b->force_params = kp;
         }
@@ -379,7 +379,7 @@ void cache_store(const TuneKey& k, const wc_tuning& t) {
     if (!f) return;
     std::fprintf(f, "%llu %llu %u %u %u %.3f %.6f %u\n", (unsigned long long)k.n, (unsigned long long)k.cells,
                  t.density_blocks_per_sm, t.force_blocks_per_sm, t.stream_blocks_per_sm, t.cell_factor, t.step_ms,
-                 t.force_variant);
+                 t.pass_variant);
     std::fclose(f);
 }
 
@@ -558,7 +558,7 @@ WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, w
         if (n) cudaMemsetAsync(d.hits, 0, sizeof(uint32_t) * MASK_WORDS * (size_t)n, b->stream);
         // the force pass variant of the scenes' flags (a fluid with the same flags gives each scene's
         // result bit for bit)
-        const int variant = (b->base[0].flags & WC_FLAG_FORCE_TEAM) ? FORCE_TEAM : FORCE_LANE;
+        const int variant = (b->base[0].flags & WC_FLAG_CELL_TEAMS) ? PASSES_TEAM : PASSES_LANE;
         b->ld = compute_launch_dims(b->device, variant);
         sph_occupancy(true, &b->max_density_blocks, &b->max_force_blocks, variant);
         b->ld.grid_density = b->ld.sms * b->max_density_blocks;
@@ -798,11 +798,11 @@ WC_API wc_status wc_batch_tune(wc_batch* b, float dt, wc_tuning* out) {
         t.density_blocks_per_sm = (uint32_t)blocks;
         WC_TRY(trial(t));
     }
-    // threads per cell of the force pass: a 32-lane team per cell or one lane per target, each
+    // threads per cell of both neighbour passes: a 32-lane team per cell or one lane per target, each
     // at its own largest residency
-    for (uint32_t variant : {(uint32_t)WC_FORCE_LANE, (uint32_t)WC_FORCE_TEAM}) {
+    for (uint32_t variant : {(uint32_t)WC_PASSES_LANE, (uint32_t)WC_PASSES_TEAM}) {
         wc_tuning t = best;
-        t.force_variant = variant;
+        t.pass_variant = variant;
         t.force_blocks_per_sm = 64;  // clamped to the variant's occupancy
         WC_TRY(trial(t));
     }

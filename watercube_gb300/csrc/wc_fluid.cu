@@ -155,7 +155,7 @@ wc_status capture_graph(wc_fluid* f, const StepInputs& in) {
     WC_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &count));
     std::vector<cudaGraphNode_t> nodes(count);
     WC_CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &count));
-    const void* force_fn = force_kernel_symbol(f->ld.force_variant);
+    const void* force_fn = force_kernel_symbol(f->ld.pass_variant);
     for (cudaGraphNode_t nd : nodes) {
         cudaGraphNodeType ty;
         WC_CUDA_TRY(cudaGraphNodeGetType(nd, &ty));
@@ -298,7 +298,7 @@ WC_API wc_status wc_fluid_create(const wc_params* p, wc_fluid** out) {
         delete f;
         return s;
     }
-    f->ld = compute_launch_dims(f->device, (f->params.flags & WC_FLAG_FORCE_TEAM) ? FORCE_TEAM : FORCE_LANE);
+    f->ld = compute_launch_dims(f->device, (f->params.flags & WC_FLAG_CELL_TEAMS) ? PASSES_TEAM : PASSES_LANE);
     f->sc = make_scene_consts(prm);
     f->in = make_step_inputs(prm, 0.0f);
     *out = f;

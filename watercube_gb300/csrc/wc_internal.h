@@ -151,11 +151,13 @@ struct DevBuffers {
     uint32_t* err;
 };
 
-// Force pass variants (threads per cell): a 32-lane team per non-empty cell that splits the
-// cell's targets into slices (FORCE_TEAM), or one lane per target (FORCE_LANE). Both replay the
-// density pass's neighbour bit strings and give the same neighbour sets; their sums differ only
-// in the order of the additions.
-enum : int { FORCE_TEAM = 0, FORCE_LANE = 1 };
+// Neighbour pass variants (threads per cell): a 32-lane team per non-empty cell that splits the
+// cell's targets into (targets x slices) and stages candidates in shared memory (PASSES_TEAM), or
+// one lane per target walking its cell's 9 candidate rows (PASSES_LANE). The density pass of a
+// variant writes its neighbour bit strings in the layout the force pass of the same variant
+// reads; both variants select the same neighbour sets, their sums differ only in the order of
+// the additions.
+enum : int { PASSES_TEAM = 0, PASSES_LANE = 1 };
 
 // Launch geometry computed once per handle.
 struct LaunchDims {
@@ -163,10 +165,10 @@ struct LaunchDims {
     int grid_stream;   // blocks for the per-particle kernels
     int grid_density;  // persistent blocks
     int grid_force;
-    int force_variant;
+    int pass_variant;
 };
 
-LaunchDims compute_launch_dims(int device, int force_variant = FORCE_LANE);
+LaunchDims compute_launch_dims(int device, int pass_variant = PASSES_LANE);
 
 // Stage launchers (wc_sort.cu, wc_sph.cu). All enqueue on `s` and never synchronise.
 void launch_bin_count(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
@@ -225,10 +227,10 @@ struct ForceKernelArgs {
 };
 
 // The kernel entry points the force node of a captured graph is recognised by.
-const void* force_kernel_symbol(int force_variant);
-const void* force_kernel_batched_symbol(int force_variant);
+const void* force_kernel_symbol(int pass_variant);
+const void* force_kernel_batched_symbol(int pass_variant);
 // Resident blocks per SM of the two neighbour passes (single-scene or batched variant).
-void sph_occupancy(bool batched, int* density_blocks, int* force_blocks, int force_variant);
+void sph_occupancy(bool batched, int* density_blocks, int* force_blocks, int pass_variant);
 
 // Internals of a wc_fluid, for the surrogate (wc_surrogate.cu), which works on a fluid's buffers.
 struct FluidInternals {

@@ -45,6 +45,7 @@ namespace {
 constexpr uint32_t IN = 32, IN_USED = 19, HID = 64, OUT = 16, MAX_AGES = 4;
 constexpr uint32_t TILE = 128;
 constexpr uint32_t MLP_THREADS = 128;
+constexpr uint32_t MLP_CTAS_PER_SM = 6;
 constexpr uint32_t TMEM_COLS = 64;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
 
@@ -336,7 +337,7 @@ __device__ __forceinline__ void mma_layer(uint32_t tmem, uint32_t a_base, uint32
 // from the judge step's buffers (src); otherwise they are rows of x_in [n x IN] (BF16). SKIP: the
 // outputs (acceleration changes, x out_scale) drive the row's skipped steps instead (skip_row).
 template <bool FUSED, bool BATCHED, bool SKIP = false>
-__global__ void __launch_bounds__(MLP_THREADS, 6) mlp_kernel(uint32_t n, const InputSrc src,
+__global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint32_t n, const InputSrc src,
                                                           const __nv_bfloat16* __restrict__ x_in,
                                                           const MlpWeights wts, float* __restrict__ out, uint32_t ldo,
                                                           uint32_t nout, float out_scale, uint32_t* __restrict__ err,
@@ -783,16 +784,13 @@ MlpWeights weights(const wc_local* s) {
     return MlpWeights{s->wb + BF_W1T, s->wb + BF_W2T, s->wb + BF_W3T, s->w + OFF_B1, s->w + OFF_B2, s->w + OFF_B3};
 }
 
-// Persistent grid of the network kernel: every resident CTA of every SM (tensor memory allows 8 of
-// 64 columns per SM; shared memory fewer), at most one per tile.
+// Persistent grid of the network kernel: MLP_CTAS_PER_SM CTAs on every SM, at most one per tile.
+// The kernel is latency-bound (three MMA round trips per tile), so every SM runs as many tiles at
+// once as fit: __launch_bounds__(128, 6) holds a thread to 85 registers, a CTA takes 32 KB of
+// shared memory and 64 of the SM's 512 tensor-memory columns.
 int mlp_grid(const wc_local* s, uint32_t n) {
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_kernel<true, false, true>, MLP_THREADS, 0);
-        per_sm = std::max(1, std::min(per_sm, 8));
-    }
     const uint32_t tiles = (n + TILE - 1) / TILE;
-    const uint32_t g = std::min<uint32_t>(tiles, (uint32_t)(s->sms * per_sm));
+    const uint32_t g = std::min<uint32_t>(tiles, (uint32_t)s->sms * MLP_CTAS_PER_SM);
     return (int)std::max(1u, g);
 }
 

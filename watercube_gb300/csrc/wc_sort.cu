@@ -4,7 +4,8 @@
 //   bin_count     count.comp:25-36     key per particle + warp-aggregated cell histogram; the
 //                                      histogram add returns an arrival rank in the cell
 //   scan_cells    linearScan.comp:15-28 single-pass exclusive scan of the histogram with
-//                                      decoupled look-back (bounded waits), fused with the
+//                                      decoupled look-back (a warp reads 32 predecessors per
+//                                      round; bounded waits), fused with the
 //                                      non-empty cell list and the histogram clear
 //   scatter_cells reorder.comp:32-45   particle index -> offsets[key] + arrival rank
 //   rank_gather   reorder.comp/sort.comp stable rank = #(members of the cell with a smaller
@@ -183,33 +184,45 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_cells_kernel(uint32_t* __re
     const unsigned long long tile_total = s_warp[NW - 1];
     const unsigned long long thread_excl = (warp ? s_warp[warp - 1] : 0ull) + x - tv;
 
-    if (tid == 0) {
+    // Look-back by warp 0: lane k reads the descriptor of tile (tile - 1 - k - 32 r) in round r; the
+    // window's values up to and including the nearest published prefix are summed. A lane whose
+    // descriptor is not yet published (and lies before that prefix) makes the warp wait, bounded.
+    if (warp == 0) {
         unsigned long long excl = 0;
         if (tile == 0) {
-            st_volatile_u64(desc, DESC_PREFIX | tile_total);
+            if (lane == 0) st_volatile_u64(desc, DESC_PREFIX | tile_total);
         } else {
-            st_volatile_u64(desc + tile, DESC_AGG | tile_total);
-            uint32_t j = tile - 1, spins = 0;
+            if (lane == 0) st_volatile_u64(desc + tile, DESC_AGG | tile_total);
             const uint32_t limit = g_scan_spin_limit;
             const bool stall = g_scan_stall != 0u;
+            int32_t j = (int32_t)tile - 1 - (int32_t)lane;
+            uint32_t spins = 0;
             for (;;) {
-                const unsigned long long d = stall ? 0ull : ld_volatile_u64(desc + j);
+                // beyond tile 0: an empty prefix, so every window ends there
+                const unsigned long long d = j < 0 ? DESC_PREFIX : (stall ? 0ull : ld_volatile_u64(desc + j));
                 const unsigned long long flag = d >> 62;
-                if (flag == 0ull) {
+                const unsigned prefix = __ballot_sync(FULL, flag == 2ull);
+                const unsigned missing = __ballot_sync(FULL, flag == 0ull);
+                const int first = prefix ? __ffs(prefix) - 1 : 32;
+                const unsigned upto = first >= 31 ? FULL : ((2u << first) - 1u);
+                if (missing & upto) {
                     if (++spins > limit) {  // bounded: report and publish what we have
-                        atomicOr(err, DEVERR_SCAN_TIMEOUT);
+                        if (lane == 0) atomicOr(err, DEVERR_SCAN_TIMEOUT);
                         break;
                     }
                     __nanosleep(64);
                     continue;
                 }
-                excl += d & DESC_VALUE;
-                if (flag == 2ull || j == 0) break;
-                --j;
+                unsigned long long v = (int)lane <= first ? (d & DESC_VALUE) : 0ull;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+                excl += v;
+                if (first < 32) break;
+                j -= 32;
             }
-            st_volatile_u64(desc + tile, DESC_PREFIX | ((excl + tile_total) & DESC_VALUE));
+            if (lane == 0) st_volatile_u64(desc + tile, DESC_PREFIX | ((excl + tile_total) & DESC_VALUE));
         }
-        s_excl = excl;
+        if (lane == 0) s_excl = excl;
     }
     __syncthreads();
     const unsigned long long pre = s_excl + thread_excl;

@@ -598,6 +598,121 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
     release_counter(counter, m, M, lane);
 }
 
+// ---- density, one lane per target -------------------------------------------------------------
+//
+// A warp takes 32 consecutive sorted slots (dynamic scheduling over chunks of 32); each lane owns
+// one target, recomputes its cell from its position (the sort's binning) and walks the 9 row
+// ranges of the cell's 27 neighbour cells, testing every candidate. Lanes of the same cell walk
+// the same candidates in step, so their loads coincide. The target's hits form its bit string in
+// its own candidate numbering (bit b of word w: candidate 32 w + b of the rows concatenated),
+// kept when it fits the slot (at most 32 MASK_WORDS candidates); the lane force pass reads it.
+
+// Rows of the 27 neighbour cells of cell (cx, cy, cz): P[r] = first candidate of row r in the
+// concatenated numbering, D[r] = first slot of row r - P[r]; returns the candidate total.
+__device__ __forceinline__ uint32_t lane_rows(const uint32_t* __restrict__ tab, uint32_t n, int32_t R, int cx, int cy,
+                                              int cz, uint32_t P[9], uint32_t D[9]) {
+    uint32_t total = 0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const int yy = cy + (r % 3) - 1, zz = cz + (r / 3) - 1;
+        uint32_t lo = 0, hi = 0;
+        if (yy >= 0 && yy < R && zz >= 0 && zz < R) {
+            const int x0 = cx > 0 ? cx - 1 : 0;
+            const int x1 = cx + 1 < R ? cx + 1 : R - 1;
+            const uint32_t row = (uint32_t)((zz * R + yy) * R);
+            hi = min(__ldg(tab + row + x1 + 1), n);
+            lo = min(__ldg(tab + row + x0), hi);
+        }
+        P[r] = total;
+        D[r] = lo - total;
+        total += hi - lo;
+    }
+    return total;
+}
+
+template <bool BATCHED>
+__global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
+    const SceneConsts sc0, const BatchTables bt, const uint32_t n, const uint32_t num_cells,
+    const float4* pos_in,  // its .w lanes are the density output: read with coherent loads
+    float* rho_out, float* p_out, const uint32_t* __restrict__ start, const uint32_t* __restrict__ cell_list,
+    uint32_t* __restrict__ num_nonempty,  // [1]: this pass's chunk counter
+    uint32_t* __restrict__ ncount, uint32_t* __restrict__ hits, uint32_t* __restrict__ err) {
+    __shared__ uint32_t s_poff[BATCHED ? MAX_SCENES + 1 : 1];
+    __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
+    if (BATCHED) {
+        for (uint32_t t = threadIdx.x; t <= bt.num_scenes; t += blockDim.x) {
+            s_poff[t] = bt.poff[t];
+            s_coff[t] = bt.coff[t];
+        }
+        __syncthreads();
+    }
+    (void)cell_list;
+    (void)num_cells;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t M = (n + 31u) >> 5;
+    uint32_t* const counter = num_nonempty + 1;
+    uint32_t m_next = lane == 0 ? atomicAdd(counter, 1u) : 0u;
+    uint32_t m = __shfl_sync(FULL, m_next, 0);
+    for (; m < M; m = __shfl_sync(FULL, m_next, 0)) {
+        if (lane == 0) m_next = atomicAdd(counter, 1u);
+        const uint32_t ti = (m << 5) + lane;
+        if (ti >= n) continue;
+        SceneConsts sc;
+        uint32_t coff = 0;
+        if (BATCHED) {
+            const uint32_t s = find_scene(s_poff, bt.num_scenes, ti);
+            sc = bt.scenes[s];
+            coff = s_coff[s];
+        } else {
+            sc = sc0;
+        }
+        const uint32_t* tab = start + coff;
+        const float4 pi = pos_in[ti];
+        int32_t cx, cy, cz;
+        const uint32_t c = bin_key(pi.x, pi.y, pi.z, sc.bin, sc.R, &cx, &cy, &cz);
+        const uint32_t cend = min(__ldg(tab + c + 1), n);
+        const uint32_t cbeg = min(__ldg(tab + c), cend);
+        if (cend - cbeg > MAX_CELL_PARTICLES) {
+            // not evaluated (see MAX_CELL_PARTICLES): NaN density and pressure, reported
+            rho_out[4 * (size_t)ti] = __int_as_float(0x7fc00000);
+            p_out[4 * (size_t)ti] = __int_as_float(0x7fc00000);
+            if (ncount) ncount[ti] = 0u;
+            if (ti == cbeg && err) atomicOr(err, DEVERR_CELL_OVERFLOW);
+            continue;
+        }
+        uint32_t P[9], D[9];
+        const uint32_t total = lane_rows(tab, n, sc.R, cx, cy, cz, P, D);
+        const bool keep = hits != nullptr && total <= 32u * (uint32_t)MASK_WORDS;
+        uint32_t* my_hits = hits ? hits + (size_t)ti * MASK_WORDS : nullptr;
+        float acc = 0.f;
+        uint32_t nh = 0, word = 0, q = 0;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const uint32_t lo = P[r] + D[r];
+            const uint32_t len = (r < 8 ? P[r + 1] : total) - P[r];
+            for (uint32_t k = lo; k < lo + len; ++k) {
+                const float4 pj = pos_in[k];
+                const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+                // d2 <= cull is the reference's sqrtf(d2) < h; the weight (cull - d2)^3 is Poly6's
+                // (h^2 - r^2)^3 with h^2 to the ulp (the target itself: r = 0)
+                const float w = sc.cull - d2;
+                if (w >= 0.f) {
+                    acc = fmaf(w * w, w, acc);
+                    ++nh;
+                    word |= 1u << (q & 31u);
+                }
+                if ((++q & 31u) == 0u) {
+                    if (keep) my_hits[(q >> 5) - 1u] = word;
+                    word = 0u;
+                }
+            }
+        }
+        if (keep && (q & 31u)) my_hits[q >> 5] = word;
+        write_density(sc, acc, nh, pi, ti, rho_out, p_out, ncount);
+    }
+    if (lane == 0 && m == M + gridDim.x * (uint32_t)WARPS - 1u) atomicExch(counter, 0u);
+}
+
 // ---- force + integration ------------------------------------------------------------------------
 
 // Accumulators of the force pass per target: NF_PLAIN for the step; with FEAT also the time
@@ -1013,12 +1128,12 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) force_kernel(const 
 // ---- force + integration, one lane per target ------------------------------------------------
 //
 // A warp takes 32 consecutive sorted slots (dynamic scheduling over chunks of 32) and each lane
-// owns one target. The lane recomputes its cell from its position (the sort's binning), the 9
-// row ranges of the cell's 27 neighbour cells in the density pass's candidate numbering, and the
-// density pass's team split of the target's chunk of the cell (its slice count S), and decodes
-// the target's bit strings (word w of slice s holds quads s + (8 w + j) S, j = 0..7) into a
-// per-lane list of neighbour slots; the list is evaluated four neighbours per round whenever it
-// fills. Targets whose bit strings the density pass did not keep test their candidates directly.
+// owns one target. The lane recomputes its cell from its position (the sort's binning) and the 9
+// row ranges of the cell's 27 neighbour cells in the density pass's candidate numbering, and
+// decodes the target's bit string from the lane density pass (bit b of word w: candidate
+// 32 w + b) into a per-lane list of neighbour slots; the list is evaluated four neighbours per
+// round whenever it fills. Targets whose bit string was not kept (more than 32 MASK_WORDS
+// candidates) test their candidates directly.
 
 constexpr uint32_t LANE_LIST = 32;  // neighbour slots a lane collects before evaluating them
 
@@ -1034,7 +1149,7 @@ __device__ __forceinline__ uint32_t slot_of(uint32_t q, const uint32_t P[9], con
 }
 
 template <bool BATCHED, bool FEAT = false>
-__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 2 : 3) force_lane_kernel(
+__global__ void __launch_bounds__(SPH_THREADS, 3) force_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const StepInputs in, const uint32_t n, const uint32_t num_cells,
     const float4* __restrict__ pos_b, const float4* __restrict__ vel_b, const uint32_t* __restrict__ ids_b,
     float4* __restrict__ pos_a, float4* __restrict__ vel_a, uint32_t* __restrict__ ids_a,
@@ -1084,56 +1199,34 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 2 : 3) force_lane_kernel(
         const uint32_t cbeg = min(__ldg(tab + c), cend);
         const uint32_t ncell = cend - cbeg;
         // rows of the 27 neighbour cells, in the density pass's candidate numbering
-        uint32_t P[9], D[9], total = 0;
-#pragma unroll
-        for (int r = 0; r < 9; ++r) {
-            const int yy = cy + (r % 3) - 1, zz = cz + (r / 3) - 1;
-            uint32_t lo = 0, hi = 0;
-            if (yy >= 0 && yy < sc.R && zz >= 0 && zz < sc.R) {
-                const int x0 = cx > 0 ? cx - 1 : 0;
-                const int x1 = cx + 1 < sc.R ? cx + 1 : sc.R - 1;
-                const uint32_t row = (uint32_t)((zz * sc.R + yy) * sc.R);
-                hi = min(__ldg(tab + row + x1 + 1), n);
-                lo = min(__ldg(tab + row + x0), hi);
-            }
-            P[r] = total;
-            D[r] = lo - total;
-            total += hi - lo;
-        }
+        uint32_t P[9], D[9];
+        const uint32_t total = lane_rows(tab, n, sc.R, cx, cy, cz, P, D);
         const bool overfull = ncell > MAX_CELL_PARTICLES;
-        // the density pass's team for this target's chunk of the cell
+        // the lane density pass's bit string: word w, bit b is candidate 32 w + b; kept when the
+        // candidates fit the slot
         const uint32_t inchunk = live && !overfull && ti >= cbeg && ti < cend;
-        const uint32_t t0 = cbeg + ((tself - cbeg) & ~31u);
-        const uint32_t nt = inchunk ? min(32u, cend - t0) : 1u;
-        const uint32_t S = (uint32_t)(32.5f * __frcp_rn((float)nt));
-        const bool single = ncell <= 32u;
-        const bool kept = hits != nullptr && (bits_fit(total, S) || mask_shape(total, S, single).ok);
-        const uint32_t IT = (((total + 3u) >> 2) + S - 1u) / S;
-        const uint32_t nwords = (IT + 7u) >> 3;
+        const bool kept = hits != nullptr && total <= 32u * (uint32_t)MASK_WORDS;
+        const uint32_t nwords = (total + 31u) >> 5;
         float f[NF] = {};
-        // candidate generator state: bit strings (w, s, word) or direct tests (q)
+        // candidate generator state: bit strings (w, word) or direct tests (q)
         bool more = inchunk && total > 0;
-        uint32_t w = 0, sl = 0, word = 0, q = 0;
+        uint32_t w = 0, word = 0, q = 0;
         if (more && kept) word = __ldg(hits + (size_t)ti * MASK_WORDS);
         for (;;) {
             uint32_t cnt = 0;
             while (more && cnt < LANE_LIST) {
                 if (kept) {
                     if (word == 0u) {
-                        if (++sl == S) {
-                            sl = 0;
-                            ++w;
-                        }
-                        if (w >= nwords) {
+                        if (++w >= nwords) {
                             more = false;
                             break;
                         }
-                        word = __ldg(hits + (size_t)ti * MASK_WORDS + w * S + sl);
+                        word = __ldg(hits + (size_t)ti * MASK_WORDS + w);
                         continue;
                     }
                     const uint32_t b = (uint32_t)__ffs(word) - 1u;
                     word &= word - 1u;
-                    const uint32_t cq = 4u * (sl + (8u * w + (b >> 2)) * S) + (b & 3u);
+                    const uint32_t cq = 32u * w + b;
                     // bits always come from this step's density pass over the same tables; the
                     // check only keeps a stage-by-stage caller's stale bits in bounds
                     if (cq < total) {
@@ -1187,17 +1280,23 @@ static_assert(arity(&force_lane_kernel<true, false>) == ForceKernelArgs::COUNT, 
 
 }  // namespace
 
-void sph_occupancy(bool batched, int* density_blocks, int* force_blocks, int force_variant) {
+void sph_occupancy(bool batched, int* density_blocks, int* force_blocks, int pass_variant) {
     int bd = 0, bf = 0;
     if (batched) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<true>, SPH_THREADS, 0);
-        if (force_variant == FORCE_LANE)
+        if (pass_variant == PASSES_LANE)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_lane_kernel<true>, SPH_THREADS, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<true>, SPH_THREADS, 0);
+        if (pass_variant == PASSES_LANE)
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_lane_kernel<true>, SPH_THREADS, 0);
         else
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<true>, SPH_THREADS, 0);
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<false>, SPH_THREADS, 0);
-        if (force_variant == FORCE_LANE)
+        if (pass_variant == PASSES_LANE)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_lane_kernel<false>, SPH_THREADS, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, density_kernel<false>, SPH_THREADS, 0);
+        if (pass_variant == PASSES_LANE)
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_lane_kernel<false>, SPH_THREADS, 0);
         else
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, force_kernel<false>, SPH_THREADS, 0);
@@ -1206,38 +1305,50 @@ void sph_occupancy(bool batched, int* density_blocks, int* force_blocks, int for
     *force_blocks = bf > 0 ? bf : 1;
 }
 
-LaunchDims compute_launch_dims(int device, int force_variant) {
+LaunchDims compute_launch_dims(int device, int pass_variant) {
     LaunchDims ld;
     cudaDeviceGetAttribute(&ld.sms, cudaDevAttrMultiProcessorCount, device);
     if (ld.sms <= 0) ld.sms = 1;
     int bd = 1, bf = 1;
-    sph_occupancy(false, &bd, &bf, force_variant);
+    sph_occupancy(false, &bd, &bf, pass_variant);
     ld.grid_density = ld.sms * bd;
     ld.grid_force = ld.sms * bf;
     ld.grid_stream = ld.sms * 8;
-    ld.force_variant = force_variant;
+    ld.pass_variant = pass_variant;
     return ld;
 }
 
+// The density pass of variant `ld.pass_variant`: its bit strings are laid out for the force pass
+// of the same variant.
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s) {
-    density_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
-        sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
-        reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty,
-        (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr, d.hits, d.err);
+    uint32_t* nc = (sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr;
+    if (ld.pass_variant == PASSES_LANE)
+        density_lane_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
+            sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
+            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, nc, d.hits, d.err);
+    else
+        density_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
+            sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
+            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, nc, d.hits, d.err);
 }
 
 void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s) {
-    density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
-        SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
-        reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
+    if (ld.pass_variant == PASSES_LANE)
+        density_lane_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
+            SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
+            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
+    else
+        density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
+            SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
+            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
 }
 
-// The force pass of variant `ld.force_variant` (FEAT: the judge steps' feature output too), on a
+// The force pass of variant `ld.pass_variant` (FEAT: the judge steps' feature output too), on a
 // persistent grid sized from that kernel's occupancy.
 template <bool BATCHED, bool FEAT>
 void launch_force_any(const DevBuffers& d, const SceneConsts& sc, const BatchTables& bt, const StepInputs& in,
                       const LaunchDims& ld, float4* feat, cudaStream_t s) {
-    const bool lane = ld.force_variant == FORCE_LANE;
+    const bool lane = ld.pass_variant == PASSES_LANE;
     int grid = ld.grid_force;
     if (FEAT) {
         // more registers per thread than the plain kernel: its own occupancy (cached per variant)
@@ -1283,12 +1394,12 @@ void launch_force_batched_feat(const DevBuffers& d, const BatchTables& bt, const
     launch_force_any<true, true>(d, SceneConsts{}, bt, in, ld, feat, s);
 }
 
-const void* force_kernel_symbol(int force_variant) {
-    return force_variant == FORCE_LANE ? reinterpret_cast<const void*>(&force_lane_kernel<false>)
+const void* force_kernel_symbol(int pass_variant) {
+    return pass_variant == PASSES_LANE ? reinterpret_cast<const void*>(&force_lane_kernel<false>)
                                        : reinterpret_cast<const void*>(&force_kernel<false>);
 }
-const void* force_kernel_batched_symbol(int force_variant) {
-    return force_variant == FORCE_LANE ? reinterpret_cast<const void*>(&force_lane_kernel<true>)
+const void* force_kernel_batched_symbol(int pass_variant) {
+    return pass_variant == PASSES_LANE ? reinterpret_cast<const void*>(&force_lane_kernel<true>)
                                        : reinterpret_cast<const void*>(&force_kernel<true>);
 }
 
