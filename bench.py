@@ -19,10 +19,12 @@ cpu_baseline  the CPU transcription of the reference's stages (oracle, FP32) on 
            (oracle/_ref, when built) or else the oracle's transcription, all threads.
 surface    surface extraction of the same state: colour field on 256^3 vertices and marching
            cubes, CUDA-event times.
-rollout    the judged rollout at the same size from the same initial state (plain SPH, the
-           learned surrogate with an SPH judge every K = 4 steps, and the stale-acceleration
-           method without the network), a bounded number of steps each; `--workload rollout1m`
-           times it alone with --steps steps.
+rollout    rollouts at the same size from the same initial state, --rollout-steps steps each:
+           plain SPH, the learned fast rollout (a judge SPH step every K = 4 steps, the network
+           predicting the skipped steps' accelerations) and the same cycles on the stale SPH
+           acceleration (the method without the network), with the judge's density error and
+           the position drift from plain SPH; the message-passing network's modes a few steps
+           each. `--workload rollout1m` times them alone with --steps steps (default 2,000).
 Multi-GPU (torchrun): every rank runs an independent replica (the path has no exchange step);
 the slowest rank's time is reported.
 """

@@ -104,3 +104,18 @@ def test_rejects_misaligned(wclib, torch):
     g = _abi.GemmDesc(m=16, n=16, k=12, k_chunk=64, a=a.data_ptr(), lda=12, b=wt.data_ptr(), ldb=12,
                       c_f32=c.data_ptr(), ldc=16)
     assert wclib.wc_nn_gemm(C.byref(g), None, None) == _abi.WC_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("m,n,k", [(58445, 128, 384), (20000, 256, 128)])
+def test_persistent_pipeline_many_tiles(wclib, torch, m, n, k):
+    """Several output tiles per CTA: the persistent kernel's operand ring wraps around many times
+    and both tensor-memory accumulators are reused (their epilogues overlap the next tile's MMAs)."""
+    a = rnd(torch, m, k, seed=11)
+    wt = rnd(torch, n, k, seed=12)
+    bias = torch.randn(n, device="cuda")
+    c = torch.zeros(m, n, device="cuda")
+    c16 = torch.zeros(m, n, dtype=torch.bfloat16, device="cuda")
+    run(wclib, torch, m=m, n=n, k=k, a=a, lda=k, b=wt, ldb=k, bias=bias, relu=1, c_f32=c, c_bf16=c16, ldc=n)
+    ref = torch.relu(a.float() @ wt.float().t() + bias)
+    close(c, ref)
+    close(c16, ref, rel=1e-3 + 2.0 ** -8)

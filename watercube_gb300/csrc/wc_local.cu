@@ -208,23 +208,30 @@ struct SkipArgs {
     uint32_t ages;
 };
 
-__device__ __forceinline__ void skip_row(const SceneConsts& c, const SkipArgs& k, uint32_t i, const float* change) {
+// The skipped steps of a cycle. change (null: the stale SPH acceleration, the method without
+// the network): the network's acceleration changes [n x ldc], of which their mean over the
+// particles, mean[0 .. 3 ages), is taken out — the changes of internal forces sum to zero, and a
+// common offset would move every particle the same way.
+template <bool BATCHED>
+__global__ void skip_cycle_kernel(uint32_t n, const SceneConsts sc0, const BatchTables bt, const SkipArgs k,
+                                  const float* __restrict__ change, uint32_t ldc, const float* __restrict__ mean) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    SceneConsts tmp;
+    const SceneConsts& c = scene_of<BATCHED>(sc0, bt, i, tmp);
     float4 p = k.pos[i], v = k.vel[i];
     k.save_pos[i] = p;
     k.save_vel[i] = v;
     if (k.ids) k.save_ids[i] = k.ids[i];
-    skip_particle(c, k.dt, k.ages, k.acc[i], change, k.pos_b[i].w, k.feat[i].w, p, v);
+    float ch[3 * MAX_AGES];
+    if (change) {
+#pragma unroll
+        for (uint32_t j = 0; j < 3 * MAX_AGES; ++j)
+            ch[j] = j < 3u * k.ages ? change[(size_t)i * ldc + j] - mean[j] : 0.f;
+    }
+    skip_particle(c, k.dt, k.ages, k.acc[i], change ? ch : nullptr, k.pos_b[i].w, k.feat[i].w, p, v);
     k.pos[i] = p;
     k.vel[i] = v;
-}
-
-// The skipped steps of a cycle without the network (the stale SPH acceleration).
-template <bool BATCHED>
-__global__ void skip_cycle_kernel(uint32_t n, const SceneConsts sc0, const BatchTables bt, const SkipArgs k) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    SceneConsts tmp;
-    skip_row(scene_of<BATCHED>(sc0, bt, i, tmp), k, i, nullptr);
 }
 
 // ---- fused per-particle network on the tensor cores -------------------------------------------
@@ -334,15 +341,17 @@ __device__ __forceinline__ void mma_layer(uint32_t tmem, uint32_t a_base, uint32
 }
 
 // out[row * ldo + j] = out_scale * y_j for j < nout (rows < n). FUSED: the inputs are computed
-// from the judge step's buffers (src); otherwise they are rows of x_in [n x IN] (BF16). SKIP: the
-// outputs (acceleration changes, x out_scale) drive the row's skipped steps instead (skip_row).
-template <bool FUSED, bool BATCHED, bool SKIP = false>
+// from the judge step's buffers (src); otherwise they are rows of x_in [n x IN] (BF16). SUMS: also
+// the CTA's column sums of the outputs, part[blockIdx.x * OUT + j] (tiles and warps added in a
+// fixed order, so the sums are reproducible).
+template <bool FUSED, bool BATCHED, bool SUMS = false>
 __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint32_t n, const InputSrc src,
                                                           const __nv_bfloat16* __restrict__ x_in,
                                                           const MlpWeights wts, float* __restrict__ out, uint32_t ldo,
                                                           uint32_t nout, float out_scale, uint32_t* __restrict__ err,
-                                                          const SkipArgs skip = SkipArgs{}) {
+                                                          float* __restrict__ part = nullptr) {
     __shared__ MlpSmem sm;
+    __shared__ float sm_sums[MLP_THREADS / 32][OUT];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_failed;
@@ -387,29 +396,19 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
     const uint32_t mb = smem_addr(&mbar);
     uint32_t phase = 0;
     const uint32_t ntiles = (n + TILE - 1) / TILE;
+    float cta_sum = 0.f;  // thread j < OUT: column j over this CTA's tiles
 
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint32_t row = tile * TILE + tid;
         const bool valid = row < n;
         // the skipped steps' state, loaded now so that the loads overlap the MMAs
-        float4 sp = make_float4(0.f, 0.f, 0.f, 0.f), sv = sp;
-        uint32_t sid = 0;
-        if (SKIP && valid) {
-            sp = skip.pos[row];
-            sv = skip.vel[row];
-            if (skip.ids) sid = skip.ids[row];
-        }
-        float4 fin_acc = make_float4(0.f, 0.f, 0.f, 0.f), fin_feat = fin_acc, fin_pos = fin_acc;
         {
             float x[IN];
             if (FUSED) {
                 if (valid) {
                     SceneConsts tmp;
                     const SceneConsts& c = scene_of<BATCHED>(src.sc, src.bt, row, tmp);
-                    fin_pos = src.pos[row];
-                    fin_acc = src.acc[row];
-                    fin_feat = src.feat[row];
-                    particle_inputs(c, src.fs, fin_pos, src.vel[row], fin_acc, fin_feat, x);
+                    particle_inputs(c, src.fs, src.pos[row], src.vel[row], src.acc[row], src.feat[row], x);
                 } else {
 #pragma unroll
                     for (int q = 0; q < (int)IN; ++q) x[q] = 0.f;
@@ -472,26 +471,27 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
         {
             float y[16];
             tmem_ld16(tlane, y);
+#pragma unroll
+            for (uint32_t j = 0; j < OUT; ++j) y[j] = (valid && ok && j < nout) ? out_scale * (y[j] + sm.b3[j]) : 0.f;
             if (valid && ok) {
-                if (SKIP) {
-                    float ch[3 * MAX_AGES];
+                float* o = out + (size_t)row * ldo;
 #pragma unroll
-                    for (uint32_t j = 0; j < 3 * MAX_AGES; ++j) ch[j] = out_scale * (y[j] + sm.b3[j]);
-                    SceneConsts tmp;
-                    const SceneConsts& c = scene_of<BATCHED>(src.sc, src.bt, row, tmp);
-                    skip.save_pos[row] = sp;
-                    skip.save_vel[row] = sv;
-                    if (skip.ids) skip.save_ids[row] = sid;
-                    skip_particle(c, skip.dt, skip.ages, fin_acc, ch, fin_pos.w, fin_feat.w, sp, sv);
-                    skip.pos[row] = sp;
-                    skip.vel[row] = sv;
-                } else {
-                    float* o = out + (size_t)row * ldo;
+                for (uint32_t j = 0; j < OUT; ++j)
+                    if (j < nout) o[j] = y[j];
+            }
+            if (SUMS) {
 #pragma unroll
-                    for (uint32_t j = 0; j < OUT; ++j)
-                        if (j < nout) o[j] = out_scale * (y[j] + sm.b3[j]);
+                for (uint32_t j = 0; j < OUT; ++j) {
+                    float v = y[j];
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+                    if (lane == 0) sm_sums[warp][j] = v;
                 }
             }
+        }
+        if (SUMS) {
+            __syncthreads();
+            if (tid < OUT) cta_sum += ((sm_sums[0][tid] + sm_sums[1][tid]) + sm_sums[2][tid]) + sm_sums[3][tid];
         }
         if (!ok) atomicOr(&s_failed, 1);
         // the next tile rewrites x and h and the accumulator
@@ -500,11 +500,28 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
         if (s_failed) break;
     }
     if (s_failed && tid == 0 && err) atomicOr(err, DEVERR_MMA_TIMEOUT);
+    if (SUMS && tid < OUT) part[(size_t)blockIdx.x * OUT + tid] = cta_sum;
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// mean[j] = (sum over CTAs of part[cta][j]) / n, j < OUT: 16 threads per column, FP64, fixed order.
+__global__ void __launch_bounds__(256) output_mean_kernel(uint32_t ctas, uint32_t n, const float* __restrict__ part,
+                                                          float* __restrict__ mean) {
+    __shared__ double s[OUT][16];
+    const uint32_t j = threadIdx.x >> 4, sub = threadIdx.x & 15u;
+    double a = 0.0;
+    for (uint32_t c = sub; c < ctas; c += 16u) a += part[(size_t)c * OUT + j];
+    s[j][sub] = a;
+    __syncthreads();
+    if (sub == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 16; ++q) t += s[j][q];
+        mean[j] = n ? (float)(t / n) : 0.f;
     }
 }
 
@@ -519,26 +536,28 @@ __global__ void copy_w_kernel(uint32_t n, const float4* __restrict__ src, float*
 // Judge: per-block sums (FP64) of |carried / rho_SPH - 1| over the sorted buffer after the
 // density pass, then one fixed-order sum of the block sums.
 constexpr uint32_t JUDGE_THREADS = 256;
+constexpr uint32_t JUDGE_BLOCKS = 512;
 __global__ void __launch_bounds__(JUDGE_THREADS) judge_partial_kernel(uint32_t n, const float* __restrict__ carried,
                                                                       const float4* __restrict__ pos_b,
                                                                       double* __restrict__ part) {
-    __shared__ double s[JUDGE_THREADS];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    double e = 0.0;
-    if (i < n) {
-        // the ratio in FP32 (relative rounding 1e-7 against a tolerance of order 1e-2), the sums
-        // in FP64
+    __shared__ double s[JUDGE_THREADS / 32];
+    // the ratio in FP32 (relative rounding 1e-7 against a tolerance of order 1e-2); a thread's
+    // few terms and a warp's sum in FP32, the rest in FP64, every sum in a fixed order
+    float e = 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float r = pos_b[i].w;
         const float q = r != 0.f ? fabsf(__fdividef(carried[i], r) - 1.f) : 0.f;
-        e = isfinite(q) ? (double)q : 1.0;
+        e += isfinite(q) ? q : 1.f;
     }
-    s[threadIdx.x] = e;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) e += __shfl_xor_sync(0xffffffffu, e, off);
+    if ((threadIdx.x & 31u) == 0) s[threadIdx.x >> 5] = e;
     __syncthreads();
-    for (uint32_t h = JUDGE_THREADS / 2; h > 0; h >>= 1) {
-        if (threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (uint32_t w = 0; w < JUDGE_THREADS / 32; ++w) a += s[w];
+        part[blockIdx.x] = a;
     }
-    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
 }
 __global__ void judge_final_kernel(uint32_t blocks, const double* __restrict__ part, double* __restrict__ out) {
     __shared__ double s[256];
@@ -712,6 +731,8 @@ struct wc_local {
     float* colsum_part = nullptr;
     // rollout scratch
     float* change = nullptr;
+    float* mean_part = nullptr;  // per-CTA column sums of the network's outputs
+    float* mean = nullptr;       // their mean over the particles [OUT]
     float* carried = nullptr;
     float4 *save_pos[2] = {nullptr, nullptr}, *save_vel[2] = {nullptr, nullptr};
     uint32_t* save_ids[2] = {nullptr, nullptr};
@@ -752,6 +773,8 @@ void free_local(wc_local* s) {
     dfree(s->loss_part);
     dfree(s->colsum_part);
     dfree(s->change);
+    dfree(s->mean_part);
+    dfree(s->mean);
     dfree(s->carried);
     dfree(s->judge_part);
     dfree(s->judge_out);
@@ -838,7 +861,7 @@ void enqueue_closing_judge(wc_local* s, const StepTarget& t) {
         launch_density_batched(d, t.bt, t.ld, t.stream);
     else
         launch_density(d, t.sc, t.ld, t.stream);
-    const uint32_t blocks = blocks_for(d.n, JUDGE_THREADS);
+    const uint32_t blocks = std::min(blocks_for(d.n, JUDGE_THREADS), JUDGE_BLOCKS);
     judge_partial_kernel<<<blocks, JUDGE_THREADS, 0, t.stream>>>(d.n, s->carried, d.pos_b, s->judge_part);
     judge_final_kernel<<<1, 256, 0, t.stream>>>(blocks, s->judge_part, s->judge_out);
 }
@@ -867,7 +890,7 @@ void enqueue_judge_step(wc_local* s, const StepTarget& t, float dt, bool judge) 
         launch_force_feat(d, t.sc, in, t.ld, s->feat, t.stream);
     }
     if (judge && d.n) {
-        const uint32_t blocks = blocks_for(d.n, JUDGE_THREADS);
+        const uint32_t blocks = std::min(blocks_for(d.n, JUDGE_THREADS), JUDGE_BLOCKS);
         judge_partial_kernel<<<blocks, JUDGE_THREADS, 0, t.stream>>>(d.n, s->carried, d.pos_b, s->judge_part);
         judge_final_kernel<<<1, 256, 0, t.stream>>>(blocks, s->judge_part, s->judge_out);
     }
@@ -1113,6 +1136,8 @@ void init_params(wc_local* s, std::vector<float>& host) {
 wc_status ensure_roll(wc_local* s, uint32_t n) {
     if (n <= s->cap_roll) return WC_OK;
     dfree(s->change);
+    dfree(s->mean_part);
+    dfree(s->mean);
     dfree(s->carried);
     dfree(s->judge_part);
     for (int q = 0; q < 2; ++q) {
@@ -1122,6 +1147,8 @@ wc_status ensure_roll(wc_local* s, uint32_t n) {
     }
     s->cap_roll = 0;
     WC_TRY(dalloc(&s->change, (size_t)n * 3u * MAX_AGES));
+    if (!s->mean_part) WC_TRY(dalloc(&s->mean_part, (size_t)s->sms * MLP_CTAS_PER_SM * OUT));
+    if (!s->mean) WC_TRY(dalloc(&s->mean, OUT));
     WC_TRY(dalloc(&s->carried, n));
     WC_TRY(dalloc(&s->judge_part, blocks_for(n, JUDGE_THREADS)));
     for (int q = 0; q < 2; ++q) {
@@ -1462,12 +1489,19 @@ WC_API wc_status wc_local_rollout(wc_local* s, wc_fluid* f, float dt, uint32_t n
         SkipArgs k{d.pos_a, d.vel_a, d.accel, w->feat, d.pos_b, w->save_pos[slot], w->save_vel[slot],
                    ids ? d.ids_a : nullptr, w->save_ids[slot], dt, count};
         if (s) {
+            // the network's changes and their mean over the particles, then the skipped steps
             cast(s);
             const InputSrc src = input_src(s, t, dt);
-            mlp_kernel<true, false, true><<<mlp_grid(s, n), MLP_THREADS, 0, t.stream>>>(
-                n, src, nullptr, weights(s), nullptr, 0, 0, s->cfg.accel_scale, s->d_err, k);
+            const int grid = mlp_grid(s, n);
+            mlp_kernel<true, false, true><<<grid, MLP_THREADS, 0, t.stream>>>(
+                n, src, nullptr, weights(s), w->change, 3u * MAX_AGES, 3u * count, s->cfg.accel_scale, s->d_err,
+                w->mean_part);
+            output_mean_kernel<<<1, 256, 0, t.stream>>>((uint32_t)grid, n, w->mean_part, w->mean);
+            skip_cycle_kernel<false><<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.sc, BatchTables{}, k, w->change,
+                                                                               3u * MAX_AGES, w->mean);
         } else {
-            skip_cycle_kernel<false><<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.sc, BatchTables{}, k);
+            skip_cycle_kernel<false><<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.sc, BatchTables{}, k, nullptr, 0,
+                                                                               nullptr);
         }
     };
     uint32_t last_skip = 0;  // skipped steps of the last cycle (judged at the end when > 0)

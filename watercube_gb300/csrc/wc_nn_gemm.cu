@@ -18,6 +18,11 @@
 //     [k x n] (the upstream gradient dY in X^T dY, and W in dY W^T).
 // Every wait on the mbarrier is bounded; a wait that runs out sets an error flag, and the
 // kernel still releases its tensor memory before it returns.
+//
+// Two kernels: gemm_pipe_kernel (persistent, warp-specialised, a 4-stage operand ring and two
+// accumulators, see below) for row-major operands without a split of K — the forward layers and
+// the input gradients; gemm_kernel (one tile per CTA, two operand buffers) for the transposed
+// weight-gradient operands and split-K.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -181,6 +186,71 @@ __device__ __forceinline__ void add_row(float x[32], const __nv_bfloat16* r, uin
     }
 }
 
+// Bias, gathered row adds, ReLU and the stores of 32 accumulator columns of one row:
+// x[0..ncols) belong to output columns col0 ..; kz: the split of the K range (partial outputs
+// split_stride apart).
+__device__ __forceinline__ void epilogue_store(const GemmArgs& g, float x[32], uint32_t row, uint32_t col0,
+                                               uint32_t ncols, uint32_t kz) {
+    if (g.bias) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if ((uint32_t)j < ncols) x[j] += __ldg(g.bias + col0 + j);
+    }
+    if (g.add1) add_row(x, g.add1 + (size_t)__ldg(g.add1_idx + row) * g.ld_add + col0, ncols);
+    if (g.add2) add_row(x, g.add2 + (size_t)__ldg(g.add2_idx + row) * g.ld_add + col0, ncols);
+    if (g.relu) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) x[j] = fmaxf(x[j], 0.f);
+    }
+    // Stores: 16-byte vectors for whole aligned segments, otherwise element by element with
+    // constant indices (the accumulator stays in registers either way).
+    if (g.c_f32) {
+        float* out = g.c_f32 + (size_t)kz * g.split_stride + (size_t)row * g.ldc + col0;
+        if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) {
+                float4* o = reinterpret_cast<float4*>(out + j);
+                float4 v = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+                if (g.accumulate) {
+                    const float4 c = *o;
+                    v.x += c.x;
+                    v.y += c.y;
+                    v.z += c.z;
+                    v.w += c.w;
+                }
+                *o = v;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if ((uint32_t)j < ncols) out[j] = g.accumulate ? out[j] + x[j] : x[j];
+        }
+    }
+    if (g.c_bf16) {
+        __nv_bfloat16* out = g.c_bf16 + (size_t)row * g.ldc + col0;
+        if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 8) {
+                __nv_bfloat162 q0 = __floats2bfloat162_rn(x[j], x[j + 1]);
+                __nv_bfloat162 q1 = __floats2bfloat162_rn(x[j + 2], x[j + 3]);
+                __nv_bfloat162 q2 = __floats2bfloat162_rn(x[j + 4], x[j + 5]);
+                __nv_bfloat162 q3 = __floats2bfloat162_rn(x[j + 6], x[j + 7]);
+                uint4 w;
+                w.x = *reinterpret_cast<uint32_t*>(&q0);
+                w.y = *reinterpret_cast<uint32_t*>(&q1);
+                w.z = *reinterpret_cast<uint32_t*>(&q2);
+                w.w = *reinterpret_cast<uint32_t*>(&q3);
+                *reinterpret_cast<uint4*>(out + j) = w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if ((uint32_t)j < ncols) out[j] = __float2bfloat16_rn(x[j]);
+        }
+    }
+
+}
+
 __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_t* err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     Tiles& t = *reinterpret_cast<Tiles*>(smem_raw);
@@ -305,74 +375,226 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (!row_ok || n0 + c0 >= g.n) continue;
-        const uint32_t ncols = min(32u, g.n - (n0 + c0));
         float x[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) x[j] = issued ? __uint_as_float(v[j]) : 0.f;
-        const uint32_t col0 = n0 + c0;
-        if (g.bias) {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if ((uint32_t)j < ncols) x[j] += __ldg(g.bias + col0 + j);
-        }
-        if (g.add1) add_row(x, g.add1 + (size_t)__ldg(g.add1_idx + row) * g.ld_add + col0, ncols);
-        if (g.add2) add_row(x, g.add2 + (size_t)__ldg(g.add2_idx + row) * g.ld_add + col0, ncols);
-        if (g.relu) {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) x[j] = fmaxf(x[j], 0.f);
-        }
-        // Stores: 16-byte vectors for whole aligned segments, otherwise element by element with
-        // constant indices (the accumulator stays in registers either way).
-        if (g.c_f32) {
-            float* out = g.c_f32 + (size_t)kz * g.split_stride + (size_t)row * g.ldc + col0;
-            if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
-#pragma unroll
-                for (int j = 0; j < 32; j += 4) {
-                    float4* o = reinterpret_cast<float4*>(out + j);
-                    float4 v = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-                    if (g.accumulate) {
-                        const float4 c = *o;
-                        v.x += c.x;
-                        v.y += c.y;
-                        v.z += c.z;
-                        v.w += c.w;
-                    }
-                    *o = v;
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if ((uint32_t)j < ncols) out[j] = g.accumulate ? out[j] + x[j] : x[j];
-            }
-        }
-        if (g.c_bf16) {
-            __nv_bfloat16* out = g.c_bf16 + (size_t)row * g.ldc + col0;
-            if (ncols == 32 && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
-#pragma unroll
-                for (int j = 0; j < 32; j += 8) {
-                    __nv_bfloat162 q0 = __floats2bfloat162_rn(x[j], x[j + 1]);
-                    __nv_bfloat162 q1 = __floats2bfloat162_rn(x[j + 2], x[j + 3]);
-                    __nv_bfloat162 q2 = __floats2bfloat162_rn(x[j + 4], x[j + 5]);
-                    __nv_bfloat162 q3 = __floats2bfloat162_rn(x[j + 6], x[j + 7]);
-                    uint4 w;
-                    w.x = *reinterpret_cast<uint32_t*>(&q0);
-                    w.y = *reinterpret_cast<uint32_t*>(&q1);
-                    w.z = *reinterpret_cast<uint32_t*>(&q2);
-                    w.w = *reinterpret_cast<uint32_t*>(&q3);
-                    *reinterpret_cast<uint4*>(out + j) = w;
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if ((uint32_t)j < ncols) out[j] = __float2bfloat16_rn(x[j]);
-            }
-        }
+        epilogue_store(g, x, row, n0 + c0, min(32u, g.n - (n0 + c0)), kz);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// ---- persistent, warp-specialised kernel (row-major A with gather / concatenation, B^T) --------
+//
+// Grid: one CTA per SM, looping over output tiles. Warps 0..3 (the producers) copy A and B slices
+// into a PIPE_STAGES-deep ring of shared-memory stages with cp.async, one commit group per stage,
+// and keep two stages in flight: after issuing stage i a thread waits for its copies of stage
+// i - 2 only, fences them into the async proxy and arrives on that stage's `full` barrier.
+// Warp 4 (lane 0) waits for `full`, issues the slice's four MMAs into one of two 128-column
+// accumulators in tensor memory and commits them to the stage's `empty` barrier (the stage may
+// be refilled) and, after a tile's last slice, to the accumulator's `acc_full` barrier. Warps
+// 5..8 wait for `acc_full`, read their 32 accumulator rows each (warp w reads lanes
+// 32 (w % 4) ..), apply the epilogue and arrive on `acc_empty`. So the copies of the next slices,
+// the MMAs of one tile and the epilogue of the previous tile overlap. Every wait is bounded; a
+// wait that runs out stops the CTA's loops (DEVERR_MMA_TIMEOUT) and the CTA still frees its
+// tensor memory.
+constexpr int PIPE_STAGES = 4;
+constexpr int PIPE_PRODUCERS = 4;  // warps 0..3 copy, warp 4 issues the MMAs, warps 5..8 drain
+constexpr int PIPE_THREADS = 32 * (PIPE_PRODUCERS + 1 + 4);
+constexpr uint32_t PIPE_TMEM_COLS = 256;
+
+struct __align__(1024) PipeStage {
+    __nv_bfloat16 a[BM * BK];
+    __nv_bfloat16 b[BN * BK];
+};
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// A producer thread's share of one slice: 16-byte copies (PIPE_PRODUCERS warps), zero-filled
+// outside the matrix.
+__device__ __forceinline__ void pipe_stage_copy(const OperandSrc& s, __nv_bfloat16* tile, uint32_t row0, uint32_t k0,
+                                                uint32_t ptid) {
+    const uint32_t base = smem_addr(tile);
+#pragma unroll 4
+    for (uint32_t id = ptid; id < (uint32_t)(BM * BK / 8); id += 32u * PIPE_PRODUCERS) {
+        const uint32_t r = id >> 3, g = id & 7u;
+        const uint32_t row = row0 + r, col = k0 + 8u * g;
+        const __nv_bfloat16* src = s.p;
+        uint32_t bytes = 0;
+        if (row < s.nrows && col < s.ncols) {
+            const uint32_t src_row = s.rows ? __ldg(s.rows + row) : row;
+            if (s.p2 && col >= s.k_split)
+                src = s.p2 + (size_t)src_row * s.ld2 + (col - s.k_split);
+            else
+                src = s.p + (size_t)src_row * s.ld + col;
+            bytes = 16;
+        }
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(base + tile_off(r, 8u * g)), "l"(src),
+                     "r"(bytes)
+                     : "memory");
+    }
+}
+
+__global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmArgs g, uint32_t* err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    PipeStage* stages = reinterpret_cast<PipeStage*>(smem_raw);
+    __shared__ uint64_t full[PIPE_STAGES], empty[PIPE_STAGES], acc_full[2], acc_empty[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_failed;
+    volatile int* failed = &s_failed;  // polled by all three roles
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t tiles_m = (g.m + BM - 1) / BM, tiles_n = (g.n + BN - 1) / BN;
+    const uint32_t ntiles = tiles_m * tiles_n;
+    const uint32_t nslices = (g.k + BK - 1) / BK;
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < PIPE_STAGES; ++q) {
+            mbar_init(&full[q], 32 * PIPE_PRODUCERS);
+            mbar_init(&empty[q], 1);
+        }
+        for (int q = 0; q < 2; ++q) {
+            mbar_init(&acc_full[q], 1);
+            mbar_init(&acc_empty[q], 4);  // one arrival per epilogue warp
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_failed = 0;
+    }
+    if (warp == PIPE_PRODUCERS) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(PIPE_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const OperandSrc A{g.a, g.a2, g.a_rows, g.lda, g.lda2, g.k_split, g.m, g.k, 0};
+    const OperandSrc B{g.b, nullptr, nullptr, g.ldb, 0u, 0u, g.n, g.k, 0};
+
+    if (warp < PIPE_PRODUCERS) {
+        // producers: stage i issued, stage i - 2 published
+        const uint32_t ptid = threadIdx.x;
+        uint32_t it = 0, published = 0;
+        for (uint32_t tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x) {
+            const uint32_t m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+            for (uint32_t sl = 0; sl < nslices; ++sl, ++it) {
+                const uint32_t st = it % PIPE_STAGES;
+                if (it >= (uint32_t)PIPE_STAGES &&
+                    !mbar_wait(smem_addr(&empty[st]), ((it / PIPE_STAGES) - 1u) & 1u)) {
+                    *failed = 1;
+                    break;
+                }
+                pipe_stage_copy(A, stages[st].a, m0, sl * BK, ptid);
+                pipe_stage_copy(B, stages[st].b, n0, sl * BK, ptid);
+                asm volatile("cp.async.commit_group;" ::: "memory");
+                if (it >= published + 2u) {
+                    asm volatile("cp.async.wait_group 2;" ::: "memory");
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_arrive(&full[published % PIPE_STAGES]);
+                    ++published;
+                }
+            }
+            if (*failed) break;
+        }
+        // the last stages
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (; published < it; ++published) mbar_arrive(&full[published % PIPE_STAGES]);
+    } else if (warp == PIPE_PRODUCERS) {
+        // MMA issue (one thread)
+        if (lane == 0) {
+            uint32_t it = 0, t = 0;
+            for (uint32_t tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x, ++t) {
+                const uint32_t b = t & 1u;
+                if (t >= 2 && !mbar_wait(smem_addr(&acc_empty[b]), ((t >> 1) - 1u) & 1u)) {
+                    *failed = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc_addr = tmem + b * (uint32_t)BN;
+                for (uint32_t sl = 0; sl < nslices; ++sl, ++it) {
+                    const uint32_t st = it % PIPE_STAGES;
+                    if (!mbar_wait(smem_addr(&full[st]), (it / PIPE_STAGES) & 1u)) {
+                        *failed = 1;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t a_base = smem_addr(stages[st].a), b_base = smem_addr(stages[st].b);
+#pragma unroll
+                    for (uint32_t j = 0; j < BK / 16; ++j) {
+                        const uint64_t ad = smem_desc(a_base + 256u * j);
+                        const uint64_t bd = smem_desc(b_base + 256u * j);
+                        const uint32_t acc = (sl > 0 || j > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc_addr),
+                            "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_addr(&empty[st]))
+                                 : "memory");
+                }
+                if (*failed) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_addr(&acc_full[b]))
+                             : "memory");
+            }
+        }
+        __syncwarp();
+    } else {
+        // epilogue: warp w reads accumulator lanes 32 (w % 4) .. + 31
+        const uint32_t quarter = warp & 3u;
+        uint32_t t = 0;
+        for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
+            const uint32_t b = t & 1u;
+            bool ok = !*failed && mbar_wait(smem_addr(&acc_full[b]), (t >> 1) & 1u);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                if (lane == 0) *failed = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+            const uint32_t row = m0 + 32u * quarter + lane;
+            const bool row_ok = row < g.m;
+            for (uint32_t c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t v[32];
+                const uint32_t taddr = tmem + ((32u * quarter) << 16) + b * (uint32_t)BN + c0;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (!row_ok || n0 + c0 >= g.n) continue;
+                float x[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) x[j] = nslices ? __uint_as_float(v[j]) : 0.f;
+                epilogue_store(g, x, row, n0 + c0, min(32u, g.n - (n0 + c0)), 0u);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
+        }
+    }
+    __syncthreads();
+    if (*failed && threadIdx.x == 0 && err) atomicOr(err, DEVERR_MMA_TIMEOUT);
+    if (warp == PIPE_PRODUCERS) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(PIPE_TMEM_COLS));
     }
 }
 
@@ -398,9 +620,28 @@ wc_status check_gemm(const GemmArgs& g) {
     return WC_OK;
 }
 
+size_t pipe_smem_bytes() { return sizeof(PipeStage) * PIPE_STAGES; }
+
 wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s) {
     const wc_status st = check_gemm(g);
     if (st != WC_OK || g.m == 0 || g.n == 0) return st;
+    if (!g.a_transposed && !g.b_rowmajor && g.k_chunk >= g.k) {
+        // row-major operands, no split of K: the persistent pipelined kernel, one CTA per SM
+        static int sms = 0;
+        if (!sms) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (sms <= 0) sms = 1;
+            cudaFuncSetAttribute(gemm_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pipe_smem_bytes());
+        }
+        const uint32_t tiles = ((g.m + BM - 1) / BM) * ((g.n + BN - 1) / BN);
+        const uint32_t grid = tiles < (uint32_t)sms ? tiles : (uint32_t)sms;
+        gemm_pipe_kernel<<<grid, PIPE_THREADS, pipe_smem_bytes(), s>>>(g, err);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(WC_ERR_CUDA, "gemm launch: %s", cudaGetErrorString(e));
+        return WC_OK;
+    }
     static bool attr_done = false;
     if (!attr_done) {
         cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());

@@ -685,29 +685,43 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
         const bool keep = hits != nullptr && total <= 32u * (uint32_t)MASK_WORDS;
         uint32_t* my_hits = hits ? hits + (size_t)ti * MASK_WORDS : nullptr;
         float acc = 0.f;
-        uint32_t nh = 0, word = 0, q = 0;
+        uint32_t nh = 0, nbits = 0, wout = 0;
+        unsigned long long buf = 0ull;  // hit bits not yet stored, candidate order
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
             const uint32_t lo = P[r] + D[r];
-            const uint32_t len = (r < 8 ? P[r + 1] : total) - P[r];
-            for (uint32_t k = lo; k < lo + len; ++k) {
-                const float4 pj = pos_in[k];
-                const float d2 = dist2(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
-                // d2 <= cull is the reference's sqrtf(d2) < h; the weight (cull - d2)^3 is Poly6's
-                // (h^2 - r^2)^3 with h^2 to the ulp (the target itself: r = 0)
-                const float w = sc.cull - d2;
-                if (w >= 0.f) {
-                    acc = fmaf(w * w, w, acc);
-                    ++nh;
-                    word |= 1u << (q & 31u);
+            const uint32_t end = lo + ((r < 8 ? P[r + 1] : total) - P[r]);
+            // four candidates per round, their loads in flight together (a short round re-reads
+            // the row's last candidate and ignores it)
+            for (uint32_t k = lo; k < end; k += 4u) {
+                const uint32_t cnt = min(4u, end - k);
+                float4 pj[4];
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) pj[u] = pos_in[min(k + u, end - 1u)];
+                uint32_t bits = 0;
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) {
+                    const float d2 = dist2(pi.x - pj[u].x, pi.y - pj[u].y, pi.z - pj[u].z);
+                    // d2 <= cull is the reference's sqrtf(d2) < h; the weight (cull - d2)^3 is
+                    // Poly6's (h^2 - r^2)^3 with h^2 to the ulp (the target itself: r = 0)
+                    const float w = sc.cull - d2;
+                    if (u < cnt && w >= 0.f) {
+                        acc = fmaf(w * w, w, acc);
+                        ++nh;
+                        bits |= 1u << u;
+                    }
                 }
-                if ((++q & 31u) == 0u) {
-                    if (keep) my_hits[(q >> 5) - 1u] = word;
-                    word = 0u;
+                buf |= (unsigned long long)bits << nbits;
+                nbits += cnt;
+                if (nbits >= 32u) {
+                    if (keep) my_hits[wout] = (uint32_t)buf;
+                    ++wout;
+                    buf >>= 32;
+                    nbits -= 32u;
                 }
             }
         }
-        if (keep && (q & 31u)) my_hits[q >> 5] = word;
+        if (keep && nbits) my_hits[wout] = (uint32_t)buf;
         write_density(sc, acc, nh, pi, ti, rho_out, p_out, ncount);
     }
     if (lane == 0 && m == M + gridDim.x * (uint32_t)WARPS - 1u) atomicExch(counter, 0u);
