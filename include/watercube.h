@@ -515,19 +515,27 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
 
 /* ---- learned fast rollout (no counterpart in the reference) ------------------------------ */
 /*
- * A per-particle network that predicts the SPH acceleration of the next K-1 steps from sums
- * the SPH step computes anyway. Every K-th step is a plain SPH step (the judge); its force pass
- * also accumulates, per particle, the time derivative of the pair terms under the neighbours'
- * relative motion (J) and the Poly6 density rate. The network maps 19 per-particle inputs
- * (the SPH acceleration, J dt, the density rate, velocity, density, pressure, six wall
- * distances, k / rho0) through two hidden layers of 64 (ReLU) to the acceleration changes of
- * ages 1 .. K-1, on the tensor cores (BF16 operands, FP32 accumulation in tensor memory). The
- * skipped steps integrate a(t) + change without sorting, and carry each particle's density by
- * its rate. The judge compares that carried density with the SPH density the next judge step
- * computes for the same particles; a cycle whose mean |rho_carried / rho_SPH - 1| exceeds the
- * tolerance is reverted: its K-1 steps are recomputed by plain SPH from the state after the
- * previous judge step.
+ * Every K-th step is a plain SPH step (the judge); its density pass also computes each
+ * particle's density and pressure rates, and its force pass the time derivative J of the SPH
+ * acceleration (the pair terms' derivatives under the particles' motion, with the neighbours'
+ * density and pressure rates; the viscosity term's neighbour-acceleration part and the wall
+ * terms' derivatives are left out). The K-1 skipped steps integrate a(t) + change_k without
+ * sorting, where change_k for the step k steps after the judge is, by mode:
+ *   WC_LOCAL_STALE    0 (the judge's acceleration held),
+ *   WC_LOCAL_TAYLOR   k dt J (first-order extrapolation),
+ *   WC_LOCAL_NETWORK  k dt J + the network's residual: a per-particle network maps 19 inputs
+ *                     (the SPH acceleration, J dt, the density rate, velocity, density, pressure,
+ *                     six wall distances, k / rho0) through two hidden layers of 64 (ReLU) to
+ *                     the residuals of ages 1 .. K-1, on the tensor cores (BF16 operands, FP32
+ *                     accumulation in tensor memory); their mean over the particles is removed.
+ * The skipped steps carry each particle's density by its rate. The judge compares that carried
+ * density with the SPH density the next judge step computes for the same particles; a cycle
+ * whose mean |rho_carried / rho_SPH - 1| exceeds the tolerance is reverted: its K-1 steps are
+ * recomputed by plain SPH from the state after the previous judge step.
  */
+#define WC_LOCAL_STALE 0
+#define WC_LOCAL_TAYLOR 1
+#define WC_LOCAL_NETWORK 2
 typedef struct wc_local wc_local;
 
 typedef struct wc_local_config {
@@ -558,18 +566,23 @@ WC_API wc_status wc_local_train(wc_local* net, uint32_t steps, uint32_t rows, fl
 /* Test hook: the loss and the gradient of every parameter ([wc_local_num_params]) on the
    training samples with the given row indices (modulo the sample count), without an update. */
 WC_API wc_status wc_local_gradients(wc_local* net, const uint32_t* rows_idx, uint32_t rows, float* grads, float* loss);
-/* Copy samples [first, first + count) of a set: inputs [count][32] and targets [count][16]
-   (acceleration changes / accel_scale; 3 per age); either pointer may be NULL. */
+/* Copy samples [first, first + count) of a set: inputs [count][32] and targets [count][16]:
+   columns 3 (k - 1) .. + 2 the residual (a(t + k) - a(t) - k dt J) / accel_scale of age k,
+   columns 13 .. 15 dt J / accel_scale; either pointer may be NULL. */
 WC_API wc_status wc_local_get_samples(wc_local* net, int held_out, uint64_t first, uint64_t count, float* inputs,
                                       float* targets);
-/* Relative L2 error of the network's prediction of the acceleration at each age, and of the
-   stale acceleration (the method without the network), over a sample set: host [ages] each. */
-WC_API wc_status wc_local_evaluate(wc_local* net, int held_out, float* err_net, float* err_stale);
-/* The network's outputs (acceleration changes, [n][4 * ages] floats, host) for the fluid's
-   current state: one judge step's inputs without advancing it (test hook of the inference). */
+/* Relative L2 error of the acceleration at each age over a sample set, host [ages] each, as
+   predicted by the network mode, the stale mode and the Taylor mode (err_taylor may be NULL). */
+WC_API wc_status wc_local_evaluate(wc_local* net, int held_out, float* err_net, float* err_stale, float* err_taylor);
+/* The network's outputs (the residuals of the acceleration changes, [n][3 * ages] floats, host)
+   for the fluid's current state: one judge step's inputs without advancing it (test hook of the
+   inference). */
 WC_API wc_status wc_local_predict(wc_local* net, wc_fluid* f, float dt, float* inputs, float* outputs);
-/* Advance the fluid nsteps as cycles of one judge SPH step and `ages` steps on predicted
-   accelerations (net = NULL: the stale SPH acceleration, the method without the network). */
+/* Advance the fluid nsteps as cycles of one judge SPH step and `ages` steps in `mode`
+   (WC_LOCAL_*; net may be NULL except for WC_LOCAL_NETWORK). */
+WC_API wc_status wc_local_rollout_mode(wc_local* net, wc_fluid* f, float dt, uint32_t nsteps, uint32_t ages,
+                                       float tolerance, int mode, wc_rollout_stats* stats);
+/* wc_local_rollout_mode with WC_LOCAL_NETWORK, or WC_LOCAL_STALE when net is NULL. */
 WC_API wc_status wc_local_rollout(wc_local* net, wc_fluid* f, float dt, uint32_t nsteps, uint32_t ages,
                                   float tolerance, wc_rollout_stats* stats);
 

@@ -1,12 +1,14 @@
 """FP64 restatement of the learned fast rollout's quantities. TEST INFRASTRUCTURE ONLY: used by
 tests/ to check the CUDA path, never by the solver.
 
-  pair_sums    the judge step's force-pass sums per particle: the SPH acceleration (the update
+  pair_sums    the judge step's pass sums per particle: the SPH acceleration (the update
                shader's pressure, viscosity and gravity terms, assets/fluid/update.comp:149-195),
-               J = d a / dt under the neighbours' relative motion with pressures and densities
-               held, and the Poly6 density rate -6 m c6 sum (cull - d2)^2 (r . (v_i - v_j)).
-               Neighbours are the pairs the solver's test selects (float32 d2 <= cull, the
-               reference's |r| < h), evaluated in float64.
+               the Poly6 density rate -6 m c6 sum (cull - d2)^2 (r . (v_i - v_j)), and
+               J = d a / dt when the positions move with their velocities and the densities and
+               pressures follow them (the density pass's rates; velocities held, so the viscosity
+               term's neighbour-acceleration part is not in J). Neighbours are the pairs the
+               solver's test selects (float32 d2 <= cull, the reference's |r| < h), evaluated in
+               float64.
   inputs       the network's 19 inputs (unrounded).
   forward      the network with the BF16 roundings of the tensor-core path (inputs, weights and
                hidden activations rounded to BF16, sums in float64).
@@ -57,7 +59,8 @@ def neighbour_pairs(pos32: np.ndarray, h: float, cull: float):
 
 def pair_sums(p, sorted_state: np.ndarray, cull: float):
     """Per particle of a sorted state (density and pressure from the density pass): the SPH
-    acceleration, J and the density rate, all float64."""
+    acceleration, J and the density rate, all float64. The equation of state's dp/drho turns
+    the density rate into the pressure rate (linear: k; cubic: 3 k rho^2 / rho0^3)."""
     x = sorted_state["position"].astype(np.float64)
     v = sorted_state["velocity"].astype(np.float64)
     rho = sorted_state["density"].astype(np.float64)
@@ -80,22 +83,28 @@ def pair_sums(p, sorted_state: np.ndarray, cull: float):
     ru = np.einsum("ij,ij->i", r, u)
     dp = ru * inv_d
     dcoef = np.where(pos_p, -pres * hd * inv_d * (2.0 + hd * inv_d), 0.0)
+    # the density pass's rates
+    w = np.maximum(float(cull) - np.einsum("ij,ij->i", r, r), 0.0)
+    rr = np.zeros(n)
+    np.add.at(rr, i, w * w * ru)
+    rate = -6.0 * m * c6 * rr
+    rho0, k = float(p.rest_density), float(p.stiffness)
+    dpdrho = np.full(n, k) if int(p.eos) == 1 else 3.0 * k * rho * rho / rho0**3  # 1: WC_EOS_LINEAR
+    pdot = dpdrho * rate
+    dpres = np.where(pos_p, (pdot[i] + pdot[j]) * 0.5 / rho[j] - pres * rate[j] / rho[j], 0.0)
     fp = np.zeros((n, 3))
     fv = np.zeros((n, 3))
     jp = np.zeros((n, 3))
     jv = np.zeros((n, 3))
-    rr = np.zeros(n)
     np.add.at(fp, i, coef[:, None] * r)
     np.add.at(fv, i, (v[j] - v[i]) * (hd / rho[j])[:, None])
-    np.add.at(jp, i, (dcoef * dp)[:, None] * r + coef[:, None] * u)
-    np.add.at(jv, i, u * (dp / rho[j])[:, None])
-    w = np.maximum(float(cull) - np.einsum("ij,ij->i", r, r), 0.0)
-    np.add.at(rr, i, w * w * ru)
+    np.add.at(jp, i, (dcoef * dp + dpres * hd * hd * inv_d)[:, None] * r + coef[:, None] * u)
+    np.add.at(jv, i, u * (dp / rho[j] + hd * rate[j] / (rho[j] * rho[j]))[:, None])
     g = np.array(list(p.gravity), np.float64)
     inv = 1.0 / (rho + 1e-16)
-    acc = (fp_scale * fp + fv_scale * fv + g[None, :] * rho[:, None]) * inv[:, None]
-    jerk = (fp_scale * jp + fv_scale * jv) * inv[:, None]
-    rate = -6.0 * m * c6 * rr
+    internal = (fp_scale * fp + fv_scale * fv) * inv[:, None]
+    acc = internal + g[None, :] * (rho * inv)[:, None]
+    jerk = (fp_scale * jp + fv_scale * jv) * inv[:, None] - (rate * inv)[:, None] * internal
     return acc, jerk, rate
 
 

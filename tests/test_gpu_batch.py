@@ -87,40 +87,45 @@ def test_workload_sample_runs(gpu):
         assert off[-1] == out.shape[0] == sum(s.num_particles for s in specs)
 
 
-def test_coarser_cells_keep_the_densities(gpu, oracle):
-    """The tuner's other cell edge, 1.25 h, regrids every scene: the 27-cell search still covers
-    every pair within h, so after one step each scene's densities (those of the step's density
-    pass, carried in the state) stay within 1e-5 of the FP64 oracle on the scene's own 1.0 h
-    grid, and the positions agree with the 1.0 h run to FP32 rounding (only the order of the
-    neighbour sums changes)."""
+def test_every_tuned_geometry_keeps_the_densities(gpu, oracle):
+    """Every geometry the tuner can pick: both cell edges (1.0 h and 1.25 h, which regrids every
+    scene; the 27-cell search still covers every pair within h) and both neighbour-pass variants
+    (a 32-lane team per cell, a lane per target). After one step each scene's densities (those of
+    the step's density pass, carried in the state) stay within 1e-5 of the FP64 oracle on the
+    scene's own 1.0 h grid, and the positions agree with the 1.0 h lane run to FP32 rounding (only
+    the order of the neighbour sums changes). Blocks per SM change nothing at all
+    (test_geometry_does_not_change_results)."""
     _, params, states = small_batch(4, seed=9)
     dt = 1e-3
     runs = {}
-    for factor in (1.0, 1.25):
-        with Batch(params, states) as b:
-            t = b.tuning()
-            t.cell_factor = factor
-            b.set_tuning(t)
-            assert b.tuning().cell_factor == factor
-            b.step(dt, 1)
-            runs[factor] = (b.particles(), b.ids(), b.offsets())
-    out, ids, off = runs[1.25]
-    base, base_ids, _ = runs[1.0]
+    for variant in (_abi.WC_PASSES_LANE, _abi.WC_PASSES_TEAM):
+        for factor in (1.0, 1.25):
+            with Batch(params, states) as b:
+                t = b.tuning()
+                t.cell_factor = factor
+                t.pass_variant = variant
+                b.set_tuning(t)
+                assert b.tuning().cell_factor == factor and b.tuning().pass_variant == variant
+                b.step(dt, 1)
+                runs[variant, factor] = (b.particles(), b.ids(), b.offsets())
+    base, base_ids, off = runs[_abi.WC_PASSES_LANE, 1.0]
     for s, (p, st) in enumerate(zip(params, states)):
         p = finalize(p)
         lo, hi = int(off[s]), int(off[s + 1])
         n = hi - lo
-        rho = np.empty(n)
-        rho[ids[lo:hi] - lo] = out["density"][lo:hi]
         o_sorted, _, o_perm, counts, offsets = oracle.sort(p, st)
         s64 = to64(o_sorted)
         oracle.density(p, s64, counts, offsets)
         rho64 = np.empty(n)
         rho64[o_perm] = s64["density"]
-        rel = np.abs(rho - rho64) / np.abs(rho64)
-        assert rel.max() <= 1e-5, (s, rel.max())
-        pos = np.empty((n, 3))
-        pos[ids[lo:hi] - lo] = out["position"][lo:hi]
         ref = np.empty((n, 3))
         ref[base_ids[lo:hi] - lo] = base["position"][lo:hi]
-        assert np.abs(pos - ref).max() <= 1e-5 * float(p.kernel_radius), s
+        for key, (out, ids, off_k) in runs.items():
+            assert int(off_k[s]) == lo and int(off_k[s + 1]) == hi
+            rho = np.empty(n)
+            rho[ids[lo:hi] - lo] = out["density"][lo:hi]
+            rel = np.abs(rho - rho64) / np.abs(rho64)
+            assert rel.max() <= 1e-5, (key, s, rel.max())
+            pos = np.empty((n, 3))
+            pos[ids[lo:hi] - lo] = out["position"][lo:hi]
+            assert np.abs(pos - ref).max() <= 1e-5 * float(p.kernel_radius), (key, s)

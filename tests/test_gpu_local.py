@@ -1,15 +1,18 @@
-"""The learned fast rollout on the GPU (csrc/wc_local.cu) against its FP64 restatement
+"""The fast rollout on the GPU (csrc/wc_local.cu) against its FP64 restatement
 (oracle/local_ref.py):
 
-  * the judge step's feature output (SPH acceleration, its relative-motion time derivative J,
-    the density rate) and the network's 19 inputs, within the BF16 rounding of the inputs;
+  * the judge step's feature output (SPH acceleration, its time derivative J with the
+    neighbours' density and pressure rates, the density rate) and the network's 19 inputs,
+    within the BF16 rounding of the inputs;
   * the fused tensor-core network (tcgen05, three layers in one kernel) against the FP64
     network with the same BF16 roundings;
   * the hand-written backward pass of a training step, per parameter block;
   * a rollout with tolerance 0 (every cycle reverted) equals plain SPH bit for bit, with and
     without the closing judge;
-  * trained on solver trajectories, the network predicts the acceleration of every age better
-    than the stale SPH acceleration (the method without it) on held-out samples.
+  * the Taylor extrapolation a + k dt J predicts the acceleration of every age better than the
+    stale SPH acceleration, and its rollout drifts less from plain SPH;
+  * trained on solver trajectories, the network (on top of the Taylor term) predicts the
+    acceleration of every age better than the stale SPH acceleration on held-out samples.
 """
 import numpy as np
 import pytest
@@ -18,7 +21,7 @@ from helpers import case, fluid
 from oracle import local_ref as L
 from oracle.oracle import to64
 from watercube_gb300 import _abi
-from watercube_gb300.local import LocalNet, rollout
+from watercube_gb300.local import WC_LOCAL_NETWORK, WC_LOCAL_STALE, WC_LOCAL_TAYLOR, LocalNet, rollout
 
 pytestmark = pytest.mark.gpu
 
@@ -53,10 +56,10 @@ def test_judge_step_inputs_and_network_against_fp64(gpu, oracle):
     assert e <= 1e-2, f"network outputs: relative L2 error {e:.2e}"
 
 
-def recorded(net, cycles=2, held_out=False, seed=0):
+def recorded(net, cycles=2, held_out=False, seed=0, start=None):
     p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
     with fluid(p, st) as f:
-        f.step(1e-3, 20 + 10 * seed)
+        f.step(1e-3, start if start is not None else 20 + 10 * seed)
         net.record(f, 1e-3, cycles, held_out)
 
 
@@ -104,12 +107,46 @@ def test_stale_rollout_is_judged_and_advances(gpu):
     assert (out["position"] >= p.wall_border).all() and (out["position"] <= p.size - p.wall_border).all()
 
 
-def test_network_beats_stale_acceleration(gpu):
+def test_network_and_taylor_beat_stale_acceleration(gpu):
+    """On the developed flow (from step 300 of the 16k dam break, when particles bounce off the
+    floor every step), held-out samples: the Taylor term beats the stale acceleration at every
+    age (the wall collisions it cannot foresee dominate the later ages) and the network trained
+    on another stretch beats the stale acceleration too."""
     with LocalNet(ages=3, seed=3, capacity=1 << 21) as net:
-        recorded(net, cycles=12, seed=0)
-        recorded(net, cycles=3, held_out=True, seed=2)
+        recorded(net, cycles=12, start=200)
+        recorded(net, cycles=3, held_out=True, start=300)
+        e_net0, e_stale, e_taylor = net.evaluate(held_out=True)
         loss = net.train(600, rows=4096, lr=2e-3)
-        assert loss[-50:].mean() < 0.5 * loss[:10].mean()
-        e_net, e_stale = net.evaluate(held_out=True)
-    print("held-out relative error, network:", e_net, "stale:", e_stale)
+        e_net, _, _ = net.evaluate(held_out=True)
+    print("loss", loss[:10].mean(), "->", loss[-50:].mean())
+    print("held-out relative error, network:", e_net, "(untrained", e_net0, ") stale:", e_stale, "taylor:", e_taylor)
+    assert loss[-50:].mean() < 0.9 * loss[:10].mean()
+    assert np.all(e_taylor < e_stale) and e_taylor[0] < 0.8 * e_stale[0], (e_taylor, e_stale)
     assert np.all(e_net < e_stale), (e_net, e_stale)
+
+
+def test_taylor_rollout_drifts_less_than_stale(gpu):
+    """40 steps in cycles of K = 4 on the 16k dam break: RMS position distance from plain SPH
+    (by particle id) of the Taylor mode below that of the stale mode; both judged, none
+    reverted, the density error within the tolerance."""
+    p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
+    dt = 1e-3
+    with fluid(p, st) as f:
+        f.step(dt, 40)
+        plain = f.particles()["position"][np.argsort(f.particle_ids())]
+    drift = {}
+    for mode in (WC_LOCAL_STALE, WC_LOCAL_TAYLOR):
+        with fluid(p, st) as f:
+            r = rollout(f, dt, 40, ages=3, tolerance=0.01, mode=mode)
+            pos = f.particles()["position"][np.argsort(f.particle_ids())]
+        assert r["judged"] == 10 and r["reverted"] == 0 and r["mean_density_error"] < 0.01, (mode, r)
+        drift[mode] = float(np.sqrt(np.mean(np.sum((pos - plain) ** 2, axis=1)))) / float(p.kernel_radius)
+    print("RMS drift from plain SPH (h):", drift)
+    assert drift[WC_LOCAL_TAYLOR] < drift[WC_LOCAL_STALE], drift
+
+
+def test_network_mode_needs_a_network(gpu):
+    p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
+    with fluid(p, st) as f:
+        with pytest.raises(_abi.WatercubeError):
+            rollout(f, 1e-3, 8, ages=3, mode=WC_LOCAL_NETWORK)

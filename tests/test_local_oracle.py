@@ -36,35 +36,33 @@ def test_backward_matches_central_differences():
 
 
 def test_pair_sums_are_the_time_derivatives():
-    """J and the density rate are d/dt of the SPH acceleration's pair sums and of the Poly6
-    density when positions move with their velocities and pressures and densities are held."""
+    """J and the density rate are d/dt of the SPH acceleration and of the Poly6 density when the
+    positions move with their velocities (velocities held) and the density pass recomputes the
+    densities and pressures of the moved state: finite differences of the FP64 oracle's density
+    pass and of the pair sums, for both equations of state."""
     scipy = pytest.importorskip("scipy")
     del scipy
-    from oracle.oracle import Oracle
-    from watercube_gb300.fluid import dam_break_params, finalize, generate_dam_break
+    from oracle.oracle import Oracle, to64
 
     o = Oracle()
-    p = o.dam_break_params(4096)
-    st = o.generate_dam_break(p, 0)
-    st["velocity"] = np.random.default_rng(1).normal(0.0, 0.3, (4096, 3)).astype(np.float32)
-    srt, _, _, counts, offsets = o.sort(p, st)
-    o.density(p, srt, counts, offsets)
-    from oracle.oracle import to64
-
-    s64 = to64(srt)
-    cull = o.cull_threshold(float(p.kernel_radius))
-    acc, jerk, rate = L.pair_sums(p, s64, cull)
-    tau = 1e-7
-    moved = s64.copy()
-    moved["position"] = s64["position"] + tau * s64["velocity"]
-    acc2, _, _ = L.pair_sums(p, moved, cull)
-    fd = (acc2 - acc) / tau
-    # pairs near |r| = h may enter or leave the sum between the two states: compare the bulk
-    err = np.linalg.norm(fd - jerk, axis=1)
-    assert np.median(err) <= 1e-3 * np.median(np.linalg.norm(jerk, axis=1))
-    # density rate against the FP64 oracle density of the moved state
-    a64, b64 = s64.copy(), moved.copy()
-    o.density(p, a64, counts, offsets)
-    o.density(p, b64, counts, offsets)
-    fdr = (b64["density"] - a64["density"]) / tau
-    assert np.median(np.abs(fdr - rate)) <= 1e-3 * np.median(np.abs(rate))
+    for eos in (1, 0):  # WC_EOS_LINEAR, WC_EOS_DESBRUN_CUBIC
+        p = o.dam_break_params(4096)
+        p.eos = eos
+        st = o.generate_dam_break(p, 0)
+        st["velocity"] = np.random.default_rng(1).normal(0.0, 0.3, (4096, 3)).astype(np.float32)
+        srt, _, _, counts, offsets = o.sort(p, st)
+        s64 = to64(srt)
+        o.density(p, s64, counts, offsets)
+        cull = o.cull_threshold(float(p.kernel_radius))
+        acc, jerk, rate = L.pair_sums(p, s64, cull)
+        tau = 1e-7
+        moved = s64.copy()
+        moved["position"] = s64["position"] + tau * s64["velocity"]
+        o.density(p, moved, counts, offsets)  # a move this small keeps every particle in its cell
+        fdr = (moved["density"] - s64["density"]) / tau
+        assert np.median(np.abs(fdr - rate)) <= 1e-3 * np.median(np.abs(rate)), eos
+        acc2, _, _ = L.pair_sums(p, moved, cull)
+        fd = (acc2 - acc) / tau
+        # pairs near |r| = h may enter or leave the sum between the two states: compare the bulk
+        err = np.linalg.norm(fd - jerk, axis=1)
+        assert np.median(err) <= 1e-3 * np.median(np.linalg.norm(jerk, axis=1)), eos

@@ -38,6 +38,9 @@ WC_FLAG_WALL_WEIGHTS = 1 << 6
 WC_FLAG_CELL_TEAMS = 1 << 7
 WC_PASSES_TEAM = 0
 WC_PASSES_LANE = 1
+WC_LOCAL_STALE = 0
+WC_LOCAL_TAYLOR = 1
+WC_LOCAL_NETWORK = 2
 WC_FLAGS_REFERENCE = WC_FLAG_WALL_DENSITY | WC_FLAG_WALL_FORCE | WC_FLAG_SPEED_CLAMP | WC_FLAG_MOUSE_FORCE
 
 WC_BUFFER_STATE = 1
@@ -314,9 +317,11 @@ def _declare(lib) -> None:
         "wc_local_train": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P]),
         "wc_local_gradients": (S, [P, P, C.c_uint32, P, P]),
         "wc_local_get_samples": (S, [P, C.c_int, C.c_uint64, C.c_uint64, P, P]),
-        "wc_local_evaluate": (S, [P, C.c_int, P, P]),
+        "wc_local_evaluate": (S, [P, C.c_int, P, P, P]),
         "wc_local_predict": (S, [P, P, C.c_float, P, P]),
         "wc_local_rollout": (S, [P, P, C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.POINTER(RolloutStats)]),
+        "wc_local_rollout_mode": (S, [P, P, C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.c_int,
+                                      C.POINTER(RolloutStats)]),
         "wc_sort_cells_noalloc": (S, [P, C.c_uint32, C.c_uint32, C.c_float, P, P, P, P, P]),
         "wc_sort_cells_noalloc_status": (S, [P]),
         "wc_set_device": (S, [C.c_int]),

@@ -170,6 +170,14 @@ struct LaunchDims {
 
 LaunchDims compute_launch_dims(int device, int pass_variant = PASSES_LANE);
 
+// The learned rollout's judge-step buffers of the force pass (sorted order): `out` receives
+// (J, density rate) per particle, `rate` holds the density pass's (density rate, pressure rate).
+struct FeatureBuffers {
+    float4* out;
+    const float2* rate;
+};
+
+
 // Stage launchers (wc_sort.cu, wc_sph.cu). All enqueue on `s` and never synchronise.
 void launch_bin_count(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
 void launch_scan_cells(const DevBuffers& d, cudaStream_t s);
@@ -178,12 +186,18 @@ void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t 
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s);
-// The force pass of a learned-rollout judge step: as launch_force(_batched), and per particle
-// feat[ti] = (d a/dt under the neighbours' relative motion, density rate) in sorted order.
+// The learned rollout's judge step runs the lane passes with their feature outputs, whatever
+// ld.pass_variant says: the density pass also writes rate[ti] = (density rate, pressure rate),
+// and the force pass reads the neighbours' rates and writes feat[ti] = (J, density rate), J the
+// time derivative of the SPH acceleration (sorted order).
+void launch_density_feat(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, float2* rate,
+                         cudaStream_t s);
+void launch_density_batched_feat(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, float2* rate,
+                                 cudaStream_t s);
 void launch_force_feat(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
-                       float4* feat, cudaStream_t s);
+                       FeatureBuffers fb, cudaStream_t s);
 void launch_force_batched_feat(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
-                               float4* feat, cudaStream_t s);
+                               FeatureBuffers fb, cudaStream_t s);
 // AoS <-> SoA for host copies through a contiguous staging buffer.
 void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, cudaStream_t s);
 void launch_soa_to_aos(const float4* pos, const float4* vel, float4* aos, uint32_t n, cudaStream_t s);
@@ -216,8 +230,8 @@ struct ForceKernelArgs {
     const uint32_t* hits;
     float4* accel;
     uint32_t* err;
-    float4* feat = nullptr;  // the feature output of the learned rollout's judge steps (unused here)
-    static constexpr int COUNT = 18;  // every parameter of force_kernel, in order
+    FeatureBuffers feat{};  // the feature buffers of the learned rollout's judge steps (unused here)
+    static constexpr int COUNT = 18;  // every parameter of force_lane_kernel, in order
     void* ptrs[COUNT];
     void bind() {
         void* p[COUNT] = {&sc,    &bt,    &in,    &n,     &num_cells, &pos_b,        &vel_b, &ids_b, &pos_a,

@@ -1,29 +1,34 @@
-// wc_local.cu — the learned fast rollout (no counterpart in the reference).
+// wc_local.cu — the fast rollout (no counterpart in the reference).
 //
-// Every K-th step is a plain SPH step, the judge. Its force pass also accumulates per particle
-// J, the time derivative of the SPH acceleration under the neighbours' relative motion
-// (pressures and densities held), and the Poly6 density rate (force_kernel<.., FEAT>). A
-// per-particle network maps 19 inputs of that step to the acceleration changes of the next
-// `ages` = K - 1 steps:
+// Every K-th step is a plain SPH step, the judge. Its density pass also computes each
+// particle's density and pressure rates (density_lane_kernel<.., FEAT>), and its force pass the
+// time derivative J of the SPH acceleration with the neighbours' rates (force_lane_kernel<..,
+// FEAT>). The K - 1 steps after it run without neighbour passes on
+//
+//   a(t + k) = a(t)                          WC_LOCAL_STALE
+//   a(t + k) = a(t) + k dt J                 WC_LOCAL_TAYLOR
+//   a(t + k) = a(t) + k dt J + a_s r_k       WC_LOCAL_NETWORK
+//
+// where r_k is a per-particle network's residual of the Taylor term, from 19 inputs of the judge
+// step (with its mean over the particles removed):
 //
 //   x  = [a / a_s, J dt / a_s, 100 rhodot dt / rho, v / v_s, rho / rho0 - 1, p / (k rho0),
 //         six wall distances / h (clipped to [0, 1]), 100 k / rho0]            (19, padded to 32)
-//   h1 = relu(W1 x + b1) (64),  h2 = relu(W2 h1 + b2) (64),  y = W3 h2 + b3 (16, 3 ages used each)
-//   a(t + k) = a(t) + a_s y[3 (k - 1) .. 3 (k - 1) + 2]
+//   h1 = relu(W1 x + b1) (64),  h2 = relu(W2 h1 + b2) (64),  r = W3 h2 + b3 (16, 3 ages used each)
 //
 // Inference is one kernel per judge step (mlp_kernel): per 128-particle tile the inputs are
 // computed into shared memory in the tensor cores' K-major core-matrix layout, and the three
 // layers run as tcgen05.mma (BF16 x BF16 -> FP32 in tensor memory), each epilogue reading the
 // accumulator with tcgen05.ld, adding the bias, applying ReLU and writing the next layer's BF16
-// operand back to shared memory. The skipped steps integrate a(t) + change without sorting and
-// carry each particle's density by its rate; the next judge step compares that carried density
-// with the SPH density of the same particles and reverts the cycle when the mean
+// operand back to shared memory. The skipped steps integrate in one kernel and carry each
+// particle's density by its rate; the next judge step compares that carried density with the
+// SPH density of the same particles and reverts the cycle when the mean
 // |rho_carried / rho_SPH - 1| exceeds the tolerance.
 //
 // Training (wc_local_record_*, wc_local_train) runs on trajectories of the solver itself:
-// samples are the judge step's inputs and the SPH accelerations of the next `ages` steps,
-// matched by particle id; the network is trained by Adam with the tcgen05 GEMM of wc_nn_gemm.cu
-// for the forward and the hand-written backward pass.
+// samples are the judge step's inputs and the residuals (a(t + k) - a(t) - k dt J) / a_s of the
+// SPH accelerations of the next `ages` steps, matched by particle id; the network is trained by
+// Adam with the tcgen05 GEMM of wc_nn_gemm.cu for the forward and the hand-written backward pass.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -206,12 +211,13 @@ struct SkipArgs {
     uint32_t* save_ids;
     float dt;
     uint32_t ages;
+    uint32_t taylor;  // add k dt J (the judge step's J, feat.xyz) to the acceleration of age k
 };
 
-// The skipped steps of a cycle. change (null: the stale SPH acceleration, the method without
-// the network): the network's acceleration changes [n x ldc], of which their mean over the
-// particles, mean[0 .. 3 ages), is taken out — the changes of internal forces sum to zero, and a
-// common offset would move every particle the same way.
+// The skipped steps of a cycle: the acceleration of age k is the judge step's, plus k dt J when
+// k.taylor is set, plus the network's residual change[i * ldc + 3 (k - 1) ..] when change is
+// given, less the residuals' mean over the particles, mean[0 .. 3 ages) (the changes of internal
+// forces sum to zero, and a common offset would move every particle the same way).
 template <bool BATCHED>
 __global__ void skip_cycle_kernel(uint32_t n, const SceneConsts sc0, const BatchTables bt, const SkipArgs k,
                                   const float* __restrict__ change, uint32_t ldc, const float* __restrict__ mean) {
@@ -223,13 +229,17 @@ __global__ void skip_cycle_kernel(uint32_t n, const SceneConsts sc0, const Batch
     k.save_pos[i] = p;
     k.save_vel[i] = v;
     if (k.ids) k.save_ids[i] = k.ids[i];
+    const float4 jf = k.feat[i];
     float ch[3 * MAX_AGES];
-    if (change) {
 #pragma unroll
-        for (uint32_t j = 0; j < 3 * MAX_AGES; ++j)
-            ch[j] = j < 3u * k.ages ? change[(size_t)i * ldc + j] - mean[j] : 0.f;
+    for (uint32_t j = 0; j < 3 * MAX_AGES; ++j) {
+        const uint32_t age = j / 3u + 1u;
+        const float jq = (j % 3u) == 0 ? jf.x : ((j % 3u) == 1 ? jf.y : jf.z);
+        float x = k.taylor ? (float)age * k.dt * jq : 0.f;
+        if (change && j < 3u * k.ages) x += change[(size_t)i * ldc + j] - mean[j];
+        ch[j] = x;
     }
-    skip_particle(c, k.dt, k.ages, k.acc[i], change ? ch : nullptr, k.pos_b[i].w, k.feat[i].w, p, v);
+    skip_particle(c, k.dt, k.ages, k.acc[i], (change || k.taylor) ? ch : nullptr, k.pos_b[i].w, jf.w, p, v);
     k.pos[i] = p;
     k.vel[i] = v;
 }
@@ -397,18 +407,35 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
     uint32_t phase = 0;
     const uint32_t ntiles = (n + TILE - 1) / TILE;
     float cta_sum = 0.f;  // thread j < OUT: column j over this CTA's tiles
+    // FUSED: this thread's row of the next tile, loaded one tile ahead so that the loads overlap
+    // the current tile's MMAs
+    float4 nx_p = make_float4(0.f, 0.f, 0.f, 0.f), nx_v = nx_p, nx_a = nx_p, nx_f = nx_p;
+    if (FUSED && (size_t)blockIdx.x * TILE + tid < n) {
+        const uint32_t r = blockIdx.x * TILE + tid;
+        nx_p = src.pos[r];
+        nx_v = src.vel[r];
+        nx_a = src.acc[r];
+        nx_f = src.feat[r];
+    }
 
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint32_t row = tile * TILE + tid;
         const bool valid = row < n;
-        // the skipped steps' state, loaded now so that the loads overlap the MMAs
         {
             float x[IN];
             if (FUSED) {
+                const float4 cp = nx_p, cv = nx_v, ca = nx_a, cf = nx_f;
+                const size_t next = (size_t)(tile + gridDim.x) * TILE + tid;
+                if (next < n) {
+                    nx_p = src.pos[next];
+                    nx_v = src.vel[next];
+                    nx_a = src.acc[next];
+                    nx_f = src.feat[next];
+                }
                 if (valid) {
                     SceneConsts tmp;
                     const SceneConsts& c = scene_of<BATCHED>(src.sc, src.bt, row, tmp);
-                    particle_inputs(c, src.fs, src.pos[row], src.vel[row], src.acc[row], src.feat[row], x);
+                    particle_inputs(c, src.fs, cp, cv, ca, cf, x);
                 } else {
 #pragma unroll
                     for (int q = 0; q < (int)IN; ++q) x[q] = 0.f;
@@ -475,9 +502,15 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
             for (uint32_t j = 0; j < OUT; ++j) y[j] = (valid && ok && j < nout) ? out_scale * (y[j] + sm.b3[j]) : 0.f;
             if (valid && ok) {
                 float* o = out + (size_t)row * ldo;
+                if ((ldo & 3u) == 0 && (nout & 3u) == 0) {  // whole 16-byte groups
 #pragma unroll
-                for (uint32_t j = 0; j < OUT; ++j)
-                    if (j < nout) o[j] = y[j];
+                    for (uint32_t j = 0; j < OUT; j += 4)
+                        if (j < nout) *reinterpret_cast<float4*>(o + j) = make_float4(y[j], y[j + 1], y[j + 2], y[j + 3]);
+                } else {
+#pragma unroll
+                    for (uint32_t j = 0; j < OUT; ++j)
+                        if (j < nout) o[j] = y[j];
+                }
             }
             if (SUMS) {
 #pragma unroll
@@ -575,22 +608,36 @@ __global__ void judge_final_kernel(uint32_t blocks, const double* __restrict__ p
 // ---- sample recording ---------------------------------------------------------------------------
 
 // a0_by_id[ids[i]] = acc[i]
-__global__ void scatter_acc_kernel(uint32_t n, const uint32_t* __restrict__ ids, const float4* __restrict__ acc,
-                                   float4* __restrict__ a0_by_id) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a0_by_id[ids[i]] = acc[i];
-}
-// y_by_id[ids[i]][3 (age - 1) ..] = (acc[i] - a0_by_id[ids[i]]) * inv_a
-__global__ void target_kernel(uint32_t n, const uint32_t* __restrict__ ids, const float4* __restrict__ acc,
-                              const float4* __restrict__ a0_by_id, uint32_t age, float inv_a, float* __restrict__ y_by_id) {
+// The judge step's acceleration and J by particle id; y_by_id[id][13 .. 15] = dt J / a_s.
+__global__ void scatter_judge_kernel(uint32_t n, const uint32_t* __restrict__ ids, const float4* __restrict__ acc,
+                                     const float4* __restrict__ feat, float dt, float inv_a,
+                                     float4* __restrict__ a0_by_id, float4* __restrict__ j0_by_id,
+                                     float* __restrict__ y_by_id) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = ids[i];
-    const float4 a = acc[i], b = a0_by_id[id];
+    const float4 j = feat[i];
+    a0_by_id[id] = acc[i];
+    j0_by_id[id] = j;
+    float* y = y_by_id + (size_t)id * OUT;
+    y[13] = j.x * dt * inv_a;
+    y[14] = j.y * dt * inv_a;
+    y[15] = j.z * dt * inv_a;
+}
+// y_by_id[ids[i]][3 (age - 1) ..] = (acc[i] - a0 - age dt J) * inv_a: the residual of the Taylor
+// extrapolation the network learns.
+__global__ void target_kernel(uint32_t n, const uint32_t* __restrict__ ids, const float4* __restrict__ acc,
+                              const float4* __restrict__ a0_by_id, const float4* __restrict__ j0_by_id, uint32_t age,
+                              float dt, float inv_a, float* __restrict__ y_by_id) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = ids[i];
+    const float4 a = acc[i], b = a0_by_id[id], j = j0_by_id[id];
+    const float kdt = (float)age * dt;
     float* y = y_by_id + (size_t)id * OUT + 3u * (age - 1u);
-    y[0] = (a.x - b.x) * inv_a;
-    y[1] = (a.y - b.y) * inv_a;
-    y[2] = (a.z - b.z) * inv_a;
+    y[0] = (a.x - fmaf(kdt, j.x, b.x)) * inv_a;
+    y[1] = (a.y - fmaf(kdt, j.y, b.y)) * inv_a;
+    y[2] = (a.z - fmaf(kdt, j.z, b.z)) * inv_a;
 }
 
 // ---- training -------------------------------------------------------------------------------------
@@ -665,15 +712,17 @@ __global__ void reduce_splits_kernel(uint32_t count, uint32_t splits, const floa
     out[i] = a;
 }
 
-// Evaluation sums per age: |pred - true|^2, |stale - true|^2 = |y|^2, |true|^2 with
-// true = a0 + y (units of a_s; a0 from the inputs' first three columns).
+// Evaluation sums per age k (units of a_s; y the residual, jd = dt J from the targets' columns
+// 13 .. 15, a0 from the inputs' first three columns): |pred - y|^2 (network mode),
+// |y + k jd|^2 (stale mode), |y|^2 (Taylor mode), |a0 + y + k jd|^2 (the acceleration).
+constexpr uint32_t EVAL_SUMS = 4;
 __global__ void eval_kernel(uint64_t rows, uint32_t ages, const __nv_bfloat16* __restrict__ xs,
                             const float* __restrict__ ys, const float* __restrict__ pred, double* __restrict__ part) {
-    __shared__ double s[3 * MAX_AGES][128];
+    __shared__ double s[EVAL_SUMS * MAX_AGES][128];
     const uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    double acc[3 * MAX_AGES];
+    double acc[EVAL_SUMS * MAX_AGES];
 #pragma unroll
-    for (int q = 0; q < 3 * (int)MAX_AGES; ++q) acc[q] = 0.0;
+    for (int q = 0; q < (int)(EVAL_SUMS * MAX_AGES); ++q) acc[q] = 0.0;
     if (r < rows) {
         const float a0[3] = {__bfloat162float(xs[r * IN + 0]), __bfloat162float(xs[r * IN + 1]),
                              __bfloat162float(xs[r * IN + 2])};
@@ -682,23 +731,26 @@ __global__ void eval_kernel(uint64_t rows, uint32_t ages, const __nv_bfloat16* _
             for (int c = 0; c < 3; ++c) {
                 const double y = ys[r * OUT + 3 * g + c];
                 const double p = pred[r * OUT + 3 * g + c];
-                const double t = a0[c] + y;
-                acc[3 * g + 0] += (p - y) * (p - y);
-                acc[3 * g + 1] += y * y;
-                acc[3 * g + 2] += t * t;
+                const double ch = y + (double)(g + 1) * ys[r * OUT + 13 + c];
+                const double t = a0[c] + ch;
+                acc[EVAL_SUMS * g + 0] += (p - y) * (p - y);
+                acc[EVAL_SUMS * g + 1] += ch * ch;
+                acc[EVAL_SUMS * g + 2] += y * y;
+                acc[EVAL_SUMS * g + 3] += t * t;
             }
         }
     }
 #pragma unroll
-    for (int q = 0; q < 3 * (int)MAX_AGES; ++q) s[q][threadIdx.x] = acc[q];
+    for (int q = 0; q < (int)(EVAL_SUMS * MAX_AGES); ++q) s[q][threadIdx.x] = acc[q];
     __syncthreads();
     for (uint32_t h = 64; h > 0; h >>= 1) {
         if (threadIdx.x < h)
-            for (int q = 0; q < 3 * (int)MAX_AGES; ++q) s[q][threadIdx.x] += s[q][threadIdx.x + h];
+            for (int q = 0; q < (int)(EVAL_SUMS * MAX_AGES); ++q) s[q][threadIdx.x] += s[q][threadIdx.x + h];
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        for (int q = 0; q < 3 * (int)MAX_AGES; ++q) part[(size_t)blockIdx.x * 3 * MAX_AGES + q] = s[q][0];
+        for (int q = 0; q < (int)(EVAL_SUMS * MAX_AGES); ++q)
+            part[(size_t)blockIdx.x * EVAL_SUMS * MAX_AGES + q] = s[q][0];
 }
 
 }  // namespace
@@ -721,7 +773,9 @@ struct wc_local {
     __nv_bfloat16* x_id = nullptr;
     float* y_id = nullptr;
     float4* a0_id = nullptr;
-    float4* feat = nullptr;
+    float4* j0_id = nullptr;  // the judge step's J by particle id (recording)
+    float4* feat = nullptr;   // judge step: (J, density rate) per sorted slot
+    float2* rate = nullptr;   // judge step's density pass: (density rate, pressure rate) per sorted slot
     uint32_t cap_n = 0;
     // training scratch
     uint32_t cap_rows = 0;
@@ -759,7 +813,9 @@ void free_local(wc_local* s) {
     dfree(s->x_id);
     dfree(s->y_id);
     dfree(s->a0_id);
+    dfree(s->j0_id);
     dfree(s->feat);
+    dfree(s->rate);
     dfree(s->xb);
     dfree(s->h1);
     dfree(s->h2);
@@ -866,7 +922,8 @@ void enqueue_closing_judge(wc_local* s, const StepTarget& t) {
     judge_final_kernel<<<1, 256, 0, t.stream>>>(blocks, s->judge_part, s->judge_out);
 }
 
-// The judge step (a plain SPH step whose force pass also writes s->feat), on the target's stream.
+// The judge step (a plain SPH step whose density pass also writes s->rate and whose force pass
+// also writes s->feat), on the target's stream.
 // When `carried` is set, the sorted buffer's densities before the density pass (the carried
 // ones) are kept there and the judge sums are enqueued after it.
 void enqueue_judge_step(wc_local* s, const StepTarget& t, float dt, bool judge) {
@@ -882,12 +939,13 @@ void enqueue_judge_step(wc_local* s, const StepTarget& t, float dt, bool judge) 
     launch_scatter(d, t.ld, t.stream);
     launch_rank_gather(d, t.ld, t.stream);
     if (judge && d.n) copy_w_kernel<<<blocks_for(d.n, 256), 256, 0, t.stream>>>(d.n, d.pos_b, s->carried);
+    const FeatureBuffers fb{s->feat, s->rate};
     if (t.bt.num_scenes) {
-        launch_density_batched(d, t.bt, t.ld, t.stream);
-        launch_force_batched_feat(d, t.bt, in, t.ld, s->feat, t.stream);
+        launch_density_batched_feat(d, t.bt, t.ld, s->rate, t.stream);
+        launch_force_batched_feat(d, t.bt, in, t.ld, fb, t.stream);
     } else {
-        launch_density(d, t.sc, t.ld, t.stream);
-        launch_force_feat(d, t.sc, in, t.ld, s->feat, t.stream);
+        launch_density_feat(d, t.sc, t.ld, s->rate, t.stream);
+        launch_force_feat(d, t.sc, in, t.ld, fb, t.stream);
     }
     if (judge && d.n) {
         const uint32_t blocks = std::min(blocks_for(d.n, JUDGE_THREADS), JUDGE_BLOCKS);
@@ -911,12 +969,16 @@ wc_status ensure_n(wc_local* s, uint32_t n) {
     dfree(s->x_id);
     dfree(s->y_id);
     dfree(s->a0_id);
+    dfree(s->j0_id);
     dfree(s->feat);
+    dfree(s->rate);
     s->cap_n = 0;
     WC_TRY(dalloc(&s->x_id, (size_t)n * IN));
     WC_TRY(dalloc(&s->y_id, (size_t)n * OUT));
     WC_TRY(dalloc(&s->a0_id, n));
+    WC_TRY(dalloc(&s->j0_id, n));
     WC_TRY(dalloc(&s->feat, n));
+    WC_TRY(dalloc(&s->rate, n));
     s->cap_n = n;
     return WC_OK;
 }
@@ -954,16 +1016,17 @@ wc_status record(wc_local* s, const StepTarget& t0, float dt, uint32_t cycles, i
                 inputs_kernel<true><<<blocks_for(n, 128), 128, 0, t.stream>>>(n, src, t.d->ids_b, s->x_id);
             else
                 inputs_kernel<false><<<blocks_for(n, 128), 128, 0, t.stream>>>(n, src, t.d->ids_b, s->x_id);
-            scatter_acc_kernel<<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.d->ids_a, t.d->accel, s->a0_id);
             cudaMemsetAsync(s->y_id, 0, sizeof(float) * (size_t)n * OUT, t.stream);
+            scatter_judge_kernel<<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.d->ids_a, t.d->accel, s->feat, dt,
+                                                                          fs.inv_a, s->a0_id, s->j0_id, s->y_id);
         }
         if (t.fluid) fluid_count_step(t.fluid);
         for (uint32_t k = 1; k <= ages && rc == WC_OK; ++k) {
             rc = plain_step(t, dt);
             if (t.fluid) fluid_count_step(t.fluid);
             if (rc == WC_OK && n)
-                target_kernel<<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.d->ids_a, t.d->accel, s->a0_id, k, fs.inv_a,
-                                                                        s->y_id);
+                target_kernel<<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.d->ids_a, t.d->accel, s->a0_id,
+                                                                        s->j0_id, k, dt, fs.inv_a, s->y_id);
         }
         if (rc != WC_OK) break;
         const uint64_t base = s->count[set];
@@ -1340,7 +1403,7 @@ WC_API wc_status wc_local_get_samples(wc_local* s, int held_out, uint64_t first,
     return WC_OK;
 }
 
-WC_API wc_status wc_local_evaluate(wc_local* s, int held_out, float* err_net, float* err_stale) {
+WC_API wc_status wc_local_evaluate(wc_local* s, int held_out, float* err_net, float* err_stale, float* err_taylor) {
     clear_error();
     if (!s || !err_net || !err_stale) return fail(WC_ERR_INVALID_ARG, "null argument");
     const int set = held_out ? 1 : 0;
@@ -1352,26 +1415,25 @@ WC_API wc_status wc_local_evaluate(wc_local* s, int held_out, float* err_net, fl
     double* part = nullptr;
     const uint32_t blocks = blocks_for(rows, 128);
     WC_TRY(dalloc(&pred, rows * OUT));
-    wc_status st = dalloc(&part, (size_t)blocks * 3 * MAX_AGES);
+    wc_status st = dalloc(&part, (size_t)blocks * EVAL_SUMS * MAX_AGES);
     if (st == WC_OK) {
         mlp_kernel<false, false><<<mlp_grid(s, (uint32_t)rows), MLP_THREADS, 0, s->stream>>>(
             (uint32_t)rows, InputSrc{}, s->xs[set], weights(s), pred, OUT, OUT, 1.0f, s->d_err);
         eval_kernel<<<blocks, 128, 0, s->stream>>>(rows, s->cfg.ages, s->xs[set], s->ys[set], pred, part);
-        std::vector<double> h((size_t)blocks * 3 * MAX_AGES);
+        std::vector<double> h((size_t)blocks * EVAL_SUMS * MAX_AGES);
         if (cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s->stream) !=
                 cudaSuccess ||
             cudaStreamSynchronize(s->stream) != cudaSuccess)
             st = fail(WC_ERR_CUDA, "evaluation copy failed");
         if (st == WC_OK) {
             for (uint32_t g = 0; g < s->cfg.ages; ++g) {
-                double e = 0.0, y = 0.0, t = 0.0;
-                for (uint32_t b = 0; b < blocks; ++b) {
-                    e += h[(size_t)b * 3 * MAX_AGES + 3 * g];
-                    y += h[(size_t)b * 3 * MAX_AGES + 3 * g + 1];
-                    t += h[(size_t)b * 3 * MAX_AGES + 3 * g + 2];
-                }
-                err_net[g] = t > 0 ? (float)std::sqrt(e / t) : 0.f;
-                err_stale[g] = t > 0 ? (float)std::sqrt(y / t) : 0.f;
+                double sum[EVAL_SUMS] = {};
+                for (uint32_t b = 0; b < blocks; ++b)
+                    for (uint32_t q = 0; q < EVAL_SUMS; ++q) sum[q] += h[((size_t)b * MAX_AGES + g) * EVAL_SUMS + q];
+                const double t = sum[3];
+                err_net[g] = t > 0 ? (float)std::sqrt(sum[0] / t) : 0.f;
+                err_stale[g] = t > 0 ? (float)std::sqrt(sum[1] / t) : 0.f;
+                if (err_taylor) err_taylor[g] = t > 0 ? (float)std::sqrt(sum[2] / t) : 0.f;
             }
         }
     }
@@ -1432,16 +1494,22 @@ WC_API wc_status wc_local_predict(wc_local* s, wc_fluid* f, float dt, float* inp
     return read_err(s);
 }
 
-WC_API wc_status wc_local_rollout(wc_local* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t ages, float tolerance,
-                                  wc_rollout_stats* out) {
+WC_API wc_status wc_local_rollout_mode(wc_local* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t ages,
+                                       float tolerance, int mode, wc_rollout_stats* out) {
     clear_error();
     WC_NVTX("wc_local_rollout");
     if (!f || !out) return fail(WC_ERR_INVALID_ARG, "null argument");
     if (!(dt > 0.f)) return fail(WC_ERR_INVALID_ARG, "dt must be > 0");
     if (ages < 1 || ages > MAX_AGES) return fail(WC_ERR_INVALID_ARG, "ages must be in 1..%u", MAX_AGES);
-    if (s && ages > s->cfg.ages) return fail(WC_ERR_INVALID_ARG, "the network predicts %u ages", s->cfg.ages);
+    if (mode != WC_LOCAL_STALE && mode != WC_LOCAL_TAYLOR && mode != WC_LOCAL_NETWORK)
+        return fail(WC_ERR_INVALID_ARG, "unknown rollout mode %d", mode);
+    if (mode == WC_LOCAL_NETWORK && !s) return fail(WC_ERR_INVALID_ARG, "the network mode needs a network");
+    if (mode == WC_LOCAL_NETWORK && ages > s->cfg.ages)
+        return fail(WC_ERR_INVALID_ARG, "the network predicts %u ages", s->cfg.ages);
+    wc_local* const net = mode == WC_LOCAL_NETWORK ? s : nullptr;
+    const uint32_t taylor = mode != WC_LOCAL_STALE ? 1u : 0u;
     std::memset(out, 0, sizeof *out);
-    // a network-less rollout (the stale method) still needs the judge's scratch: a private one
+    // a rollout without a network handle still needs the judge's scratch: a private one
     wc_local* own = nullptr;
     if (!s) {
         wc_local_config c;
@@ -1487,15 +1555,15 @@ WC_API wc_status wc_local_rollout(wc_local* s, wc_fluid* f, float dt, uint32_t n
     auto skip_steps = [&](uint32_t count, int slot) {
         if (!n || !count) return;
         SkipArgs k{d.pos_a, d.vel_a, d.accel, w->feat, d.pos_b, w->save_pos[slot], w->save_vel[slot],
-                   ids ? d.ids_a : nullptr, w->save_ids[slot], dt, count};
-        if (s) {
-            // the network's changes and their mean over the particles, then the skipped steps
-            cast(s);
-            const InputSrc src = input_src(s, t, dt);
-            const int grid = mlp_grid(s, n);
+                   ids ? d.ids_a : nullptr, w->save_ids[slot], dt, count, taylor};
+        if (net) {
+            // the network's residuals and their mean over the particles, then the skipped steps
+            cast(net);
+            const InputSrc src = input_src(net, t, dt);
+            const int grid = mlp_grid(net, n);
             mlp_kernel<true, false, true><<<grid, MLP_THREADS, 0, t.stream>>>(
-                n, src, nullptr, weights(s), w->change, 3u * MAX_AGES, 3u * count, s->cfg.accel_scale, s->d_err,
-                w->mean_part);
+                n, src, nullptr, weights(net), w->change, 3u * MAX_AGES, 3u * MAX_AGES, net->cfg.accel_scale, net->d_err,
+                w->mean_part);  // all 3 MAX_AGES columns (whole 16-byte stores); the skipped steps read 3 count
             output_mean_kernel<<<1, 256, 0, t.stream>>>((uint32_t)grid, n, w->mean_part, w->mean);
             skip_cycle_kernel<false><<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.sc, BatchTables{}, k, w->change,
                                                                                3u * MAX_AGES, w->mean);
@@ -1589,6 +1657,11 @@ WC_API wc_status wc_local_rollout(wc_local* s, wc_fluid* f, float dt, uint32_t n
     out->mean_density_error = out->judged ? err_sum / out->judged : 0.0;
     out->max_density_error = err_max;
     return WC_OK;
+}
+
+WC_API wc_status wc_local_rollout(wc_local* s, wc_fluid* f, float dt, uint32_t nsteps, uint32_t ages, float tolerance,
+                                  wc_rollout_stats* out) {
+    return wc_local_rollout_mode(s, f, dt, nsteps, ages, tolerance, s ? WC_LOCAL_NETWORK : WC_LOCAL_STALE, out);
 }
 
 }  // extern "C"

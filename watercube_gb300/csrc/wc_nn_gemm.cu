@@ -19,9 +19,9 @@
 // Every wait on the mbarrier is bounded; a wait that runs out sets an error flag, and the
 // kernel still releases its tensor memory before it returns.
 //
-// Two kernels: gemm_pipe_kernel (persistent, warp-specialised, a 4-stage operand ring and two
-// accumulators, see below) for row-major operands without a split of K — the forward layers and
-// the input gradients; gemm_kernel (one tile per CTA, two operand buffers) for the transposed
+// Two kernels: gemm_pipe_kernel (persistent, warp-specialised, an operand ring, B resident in
+// shared memory when it fits, two accumulators, see below) for row-major operands without a
+// split of K — the forward layers and the input gradients; gemm_kernel (one tile per CTA, two operand buffers) for the transposed
 // weight-gradient operands and split-K.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -390,26 +390,31 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
 
 // ---- persistent, warp-specialised kernel (row-major A with gather / concatenation, B^T) --------
 //
-// Grid: one CTA per SM, looping over output tiles. Warps 0..3 (the producers) copy A and B slices
-// into a PIPE_STAGES-deep ring of shared-memory stages with cp.async, one commit group per stage,
-// and keep two stages in flight: after issuing stage i a thread waits for its copies of stage
-// i - 2 only, fences them into the async proxy and arrives on that stage's `full` barrier.
-// Warp 4 (lane 0) waits for `full`, issues the slice's four MMAs into one of two 128-column
-// accumulators in tensor memory and commits them to the stage's `empty` barrier (the stage may
-// be refilled) and, after a tile's last slice, to the accumulator's `acc_full` barrier. Warps
-// 5..8 wait for `acc_full`, read their 32 accumulator rows each (warp w reads lanes
-// 32 (w % 4) ..), apply the epilogue and arrive on `acc_empty`. So the copies of the next slices,
-// the MMAs of one tile and the epilogue of the previous tile overlap. Every wait is bounded; a
-// wait that runs out stops the CTA's loops (DEVERR_MMA_TIMEOUT) and the CTA still frees its
-// tensor memory.
-constexpr int PIPE_STAGES = 4;
+// Grid: one CTA per SM, looping over output tiles. Warps 0..3 (the producers) copy operand
+// slices with cp.async into a ring of shared-memory slots, one commit group per ring step, and
+// keep LAG groups in flight: after committing a group a thread waits until only the LAG newest
+// are pending, fences the older ones into the async proxy and arrives on their `full` barriers.
+// With B resident (RB: n <= 128 and k <= 384) the producers first copy the whole B^T tile once
+// (barrier `b_full`) and the ring carries A slices only (6 slots, 4 in flight); otherwise each
+// slot holds an A and a B slice (4 slots, 2 in flight). Warp 4 (lane 0) waits for `full`, issues
+// the slice's four MMAs into one of two 128-column accumulators in tensor memory and commits them
+// to the slot's `empty` barrier (the slot may be refilled) and, after a tile's last slice, to the
+// accumulator's `acc_full` barrier. Warps 5..8 wait for `acc_full`, read their 32 accumulator
+// rows each (warp w reads lanes 32 (w % 4) ..), apply the epilogue and arrive on `acc_empty`. So
+// the copies of the next slices, the MMAs of one tile and the epilogue of the previous tile
+// overlap. Every wait is bounded; a wait that runs out stops the CTA's loops
+// (DEVERR_MMA_TIMEOUT) and the CTA still frees its tensor memory.
 constexpr int PIPE_PRODUCERS = 4;  // warps 0..3 copy, warp 4 issues the MMAs, warps 5..8 drain
 constexpr int PIPE_THREADS = 32 * (PIPE_PRODUCERS + 1 + 4);
 constexpr uint32_t PIPE_TMEM_COLS = 256;
-
-struct __align__(1024) PipeStage {
-    __nv_bfloat16 a[BM * BK];
-    __nv_bfloat16 b[BN * BK];
+constexpr uint32_t TILE_BYTES = BM * BK * 2;  // one 128 x 64 BF16 operand slice, 16 KB
+// Resident B (RB): the whole B^T tile [128 x k] stays in shared memory, loaded once per CTA,
+// and the ring carries A slices only. For n <= 128 (one column of tiles) and k <= 64 RB_MAX_SLICES.
+constexpr uint32_t RB_MAX_SLICES = 6;
+template <bool RB>
+struct PipeShape {
+    static constexpr int STAGES = RB ? 6 : 4;  // ring slots
+    static constexpr int LAG = STAGES - 2;     // copy groups a producer keeps in flight
 };
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -444,10 +449,11 @@ __device__ __forceinline__ void pipe_stage_copy(const OperandSrc& s, __nv_bfloat
     }
 }
 
+template <bool RB>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmArgs g, uint32_t* err) {
+    constexpr int STAGES = PipeShape<RB>::STAGES, LAG = PipeShape<RB>::LAG;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    PipeStage* stages = reinterpret_cast<PipeStage*>(smem_raw);
-    __shared__ uint64_t full[PIPE_STAGES], empty[PIPE_STAGES], acc_full[2], acc_empty[2];
+    __shared__ uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], b_full;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_failed;
     volatile int* failed = &s_failed;  // polled by all three roles
@@ -455,9 +461,15 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
     const uint32_t tiles_m = (g.m + BM - 1) / BM, tiles_n = (g.n + BN - 1) / BN;
     const uint32_t ntiles = tiles_m * tiles_n;
     const uint32_t nslices = (g.k + BK - 1) / BK;
+    // RB: [B slices 0 .. nslices)[A ring]; otherwise the ring's slots hold an A and a B slice each
+    unsigned char* const ring = smem_raw + (RB ? nslices * TILE_BYTES : 0u);
+    auto a_slot = [&](uint32_t st) { return ring + st * (RB ? 1u : 2u) * TILE_BYTES; };
+    auto b_slice = [&](uint32_t st, uint32_t sl) {
+        return RB ? smem_raw + sl * TILE_BYTES : ring + (2u * st + 1u) * TILE_BYTES;
+    };
 
     if (threadIdx.x == 0) {
-        for (int q = 0; q < PIPE_STAGES; ++q) {
+        for (int q = 0; q < STAGES; ++q) {
             mbar_init(&full[q], 32 * PIPE_PRODUCERS);
             mbar_init(&empty[q], 1);
         }
@@ -465,6 +477,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
             mbar_init(&acc_full[q], 1);
             mbar_init(&acc_empty[q], 4);  // one arrival per epilogue warp
         }
+        mbar_init(&b_full, 32 * PIPE_PRODUCERS);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_failed = 0;
     }
@@ -481,38 +494,54 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
     const OperandSrc B{g.b, nullptr, nullptr, g.ldb, 0u, 0u, g.n, g.k, 0};
 
     if (warp < PIPE_PRODUCERS) {
-        // producers: stage i issued, stage i - 2 published
+        // producers: copy groups in commit order (RB: group 0 is B, group 1 + i the A slice of
+        // ring step i; otherwise group i is ring step i); a group is published (fenced, its
+        // barrier arrived on) once LAG later groups have been committed, or at the end
         const uint32_t ptid = threadIdx.x;
-        uint32_t it = 0, published = 0;
+        uint32_t it = 0, committed = 0, published = 0;
+        auto publish_upto = [&](uint32_t upto) {
+            for (; published < upto; ++published) {
+                if (RB && published == 0)
+                    mbar_arrive(&b_full);
+                else
+                    mbar_arrive(&full[(published - (RB ? 1u : 0u)) % STAGES]);
+            }
+        };
+        if (RB) {
+            for (uint32_t sl = 0; sl < nslices; ++sl)
+                pipe_stage_copy(B, reinterpret_cast<__nv_bfloat16*>(b_slice(0, sl)), 0u, sl * BK, ptid);
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            ++committed;
+        }
         for (uint32_t tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x) {
             const uint32_t m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
             for (uint32_t sl = 0; sl < nslices; ++sl, ++it) {
-                const uint32_t st = it % PIPE_STAGES;
-                if (it >= (uint32_t)PIPE_STAGES &&
-                    !mbar_wait(smem_addr(&empty[st]), ((it / PIPE_STAGES) - 1u) & 1u)) {
+                const uint32_t st = it % STAGES;
+                if (it >= (uint32_t)STAGES && !mbar_wait(smem_addr(&empty[st]), ((it / STAGES) - 1u) & 1u)) {
                     *failed = 1;
                     break;
                 }
-                pipe_stage_copy(A, stages[st].a, m0, sl * BK, ptid);
-                pipe_stage_copy(B, stages[st].b, n0, sl * BK, ptid);
+                pipe_stage_copy(A, reinterpret_cast<__nv_bfloat16*>(a_slot(st)), m0, sl * BK, ptid);
+                if (!RB) pipe_stage_copy(B, reinterpret_cast<__nv_bfloat16*>(b_slice(st, sl)), n0, sl * BK, ptid);
                 asm volatile("cp.async.commit_group;" ::: "memory");
-                if (it >= published + 2u) {
-                    asm volatile("cp.async.wait_group 2;" ::: "memory");
+                ++committed;
+                if (committed > (uint32_t)LAG) {
+                    asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_arrive(&full[published % PIPE_STAGES]);
-                    ++published;
+                    publish_upto(committed - LAG);
                 }
             }
             if (*failed) break;
         }
-        // the last stages
+        // the last groups
         asm volatile("cp.async.wait_group 0;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (; published < it; ++published) mbar_arrive(&full[published % PIPE_STAGES]);
+        publish_upto(committed);
     } else if (warp == PIPE_PRODUCERS) {
         // MMA issue (one thread)
         if (lane == 0) {
             uint32_t it = 0, t = 0;
+            if (RB && ntiles > blockIdx.x && !mbar_wait(smem_addr(&b_full), 0u)) *failed = 1;
             for (uint32_t tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x, ++t) {
                 const uint32_t b = t & 1u;
                 if (t >= 2 && !mbar_wait(smem_addr(&acc_empty[b]), ((t >> 1) - 1u) & 1u)) {
@@ -522,13 +551,13 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t acc_addr = tmem + b * (uint32_t)BN;
                 for (uint32_t sl = 0; sl < nslices; ++sl, ++it) {
-                    const uint32_t st = it % PIPE_STAGES;
-                    if (!mbar_wait(smem_addr(&full[st]), (it / PIPE_STAGES) & 1u)) {
+                    const uint32_t st = it % STAGES;
+                    if (!mbar_wait(smem_addr(&full[st]), (it / STAGES) & 1u)) {
                         *failed = 1;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t a_base = smem_addr(stages[st].a), b_base = smem_addr(stages[st].b);
+                    const uint32_t a_base = smem_addr(a_slot(st)), b_base = smem_addr(b_slice(st, sl));
 #pragma unroll
                     for (uint32_t j = 0; j < BK / 16; ++j) {
                         const uint64_t ad = smem_desc(a_base + 256u * j);
@@ -620,24 +649,37 @@ wc_status check_gemm(const GemmArgs& g) {
     return WC_OK;
 }
 
-size_t pipe_smem_bytes() { return sizeof(PipeStage) * PIPE_STAGES; }
+// Dynamic shared memory of gemm_pipe_kernel<RB> for k (RB: the resident B slices and the ring).
+size_t pipe_smem_bytes(bool rb, uint32_t k) {
+    const uint32_t nslices = (k + BK - 1) / BK;
+    return rb ? (size_t)(nslices + PipeShape<true>::STAGES) * TILE_BYTES
+              : (size_t)PipeShape<false>::STAGES * 2u * TILE_BYTES;
+}
 
 wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s) {
     const wc_status st = check_gemm(g);
     if (st != WC_OK || g.m == 0 || g.n == 0) return st;
     if (!g.a_transposed && !g.b_rowmajor && g.k_chunk >= g.k) {
-        // row-major operands, no split of K: the persistent pipelined kernel, one CTA per SM
+        // row-major operands, no split of K: the persistent pipelined kernel, one CTA per SM;
+        // B resident in shared memory when it is one column of tiles of at most RB_MAX_SLICES
         static int sms = 0;
         if (!sms) {
             int dev = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             if (sms <= 0) sms = 1;
-            cudaFuncSetAttribute(gemm_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pipe_smem_bytes());
+            cudaFuncSetAttribute(gemm_pipe_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)pipe_smem_bytes(false, 0));
+            cudaFuncSetAttribute(gemm_pipe_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)pipe_smem_bytes(true, RB_MAX_SLICES * BK));
         }
         const uint32_t tiles = ((g.m + BM - 1) / BM) * ((g.n + BN - 1) / BN);
         const uint32_t grid = tiles < (uint32_t)sms ? tiles : (uint32_t)sms;
-        gemm_pipe_kernel<<<grid, PIPE_THREADS, pipe_smem_bytes(), s>>>(g, err);
+        const bool rb = g.n <= (uint32_t)BN && (g.k + BK - 1) / BK <= RB_MAX_SLICES;
+        if (rb)
+            gemm_pipe_kernel<true><<<grid, PIPE_THREADS, pipe_smem_bytes(true, g.k), s>>>(g, err);
+        else
+            gemm_pipe_kernel<false><<<grid, PIPE_THREADS, pipe_smem_bytes(false, g.k), s>>>(g, err);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return fail(WC_ERR_CUDA, "gemm launch: %s", cudaGetErrorString(e));
         return WC_OK;

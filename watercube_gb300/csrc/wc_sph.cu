@@ -401,6 +401,24 @@ __device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, 
     if (ncount) ncount[ti] = hits - 1u;
 }
 
+// The judge step's rates of one particle from its density-pass sums: the Poly6 density rate
+// -6 m c6 sum (cull - d2)^2 (r . u) (the time derivative of m c6 sum (cull - d2)^3 with
+// d(d2)/dt = 2 r . u), and the pressure rate dp/drho times it for the equation of state. The
+// wall terms (wall weights, pseudo wall density) are left out of both.
+__device__ __forceinline__ void write_rates(const SceneConsts& sc, float sum, float rr, uint32_t ti,
+                                            float2* rate_out) {
+    const float rho = (sc.m * sc.c6) * sum;
+    const float rate = -6.f * sc.m * sc.c6 * rr;
+    float dp;
+    if (sc.eos == WC_EOS_LINEAR) {
+        dp = sc.k;
+    } else {
+        const float x = rho / sc.rho0;
+        dp = 3.f * sc.k * x * x / sc.rho0;
+    }
+    rate_out[ti] = make_float2(rate, dp * rate);
+}
+
 // Dynamic cell scheduling: every warp takes cells from a counter until it draws an index >= M,
 // so a launch of W warps hands out exactly M + W indices and each warp's last draw is one of
 // M .. M + W - 1. The warp that draws M + W - 1 draws last; it puts the counter back to zero for
@@ -606,6 +624,8 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
 // the same candidates in step, so their loads coincide. The target's hits form its bit string in
 // its own candidate numbering (bit b of word w: candidate 32 w + b of the rows concatenated),
 // kept when it fits the slot (at most 32 MASK_WORDS candidates); the lane force pass reads it.
+// FEAT (the learned rollout's judge steps): each hit also adds (cull - d2)^2 (r . u), u = v_i - v_j,
+// to the Poly6 density rate, and the pass writes rate_out[ti] = (density rate, pressure rate).
 
 // Rows of the 27 neighbour cells of cell (cx, cy, cz): P[r] = first candidate of row r in the
 // concatenated numbering, D[r] = first slot of row r - P[r]; returns the candidate total.
@@ -630,13 +650,15 @@ __device__ __forceinline__ uint32_t lane_rows(const uint32_t* __restrict__ tab, 
     return total;
 }
 
-template <bool BATCHED>
-__global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
+template <bool BATCHED, bool FEAT = false>
+__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) density_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const uint32_t n, const uint32_t num_cells,
     const float4* pos_in,  // its .w lanes are the density output: read with coherent loads
     float* rho_out, float* p_out, const uint32_t* __restrict__ start, const uint32_t* __restrict__ cell_list,
     uint32_t* __restrict__ num_nonempty,  // [1]: this pass's chunk counter
-    uint32_t* __restrict__ ncount, uint32_t* __restrict__ hits, uint32_t* __restrict__ err) {
+    uint32_t* __restrict__ ncount, uint32_t* __restrict__ hits, uint32_t* __restrict__ err,
+    const float4* vel_in = nullptr,  // FEAT: velocities (their .w lanes are the pressure output)
+    float2* __restrict__ rate_out = nullptr) {
     __shared__ uint32_t s_poff[BATCHED ? MAX_SCENES + 1 : 1];
     __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
     if (BATCHED) {
@@ -677,6 +699,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
             rho_out[4 * (size_t)ti] = __int_as_float(0x7fc00000);
             p_out[4 * (size_t)ti] = __int_as_float(0x7fc00000);
             if (ncount) ncount[ti] = 0u;
+            if (FEAT) rate_out[ti] = make_float2(0.f, 0.f);
             if (ti == cbeg && err) atomicOr(err, DEVERR_CELL_OVERFLOW);
             continue;
         }
@@ -684,6 +707,9 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
         const uint32_t total = lane_rows(tab, n, sc.R, cx, cy, cz, P, D);
         const bool keep = hits != nullptr && total <= 32u * (uint32_t)MASK_WORDS;
         uint32_t* my_hits = hits ? hits + (size_t)ti * MASK_WORDS : nullptr;
+        float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (FEAT) vi = vel_in[ti];
+        float rr = 0.f;  // FEAT: sum of (cull - d2)^2 (r . u)
         float acc = 0.f;
         uint32_t nh = 0, nbits = 0, wout = 0;
         unsigned long long buf = 0ull;  // hit bits not yet stored, candidate order
@@ -709,6 +735,12 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
                         acc = fmaf(w * w, w, acc);
                         ++nh;
                         bits |= 1u << u;
+                        if (FEAT) {
+                            const float4 vj = vel_in[k + u];
+                            const float ru = fmaf(pi.z - pj[u].z, vi.z - vj.z,
+                                                  fmaf(pi.y - pj[u].y, vi.y - vj.y, (pi.x - pj[u].x) * (vi.x - vj.x)));
+                            rr = fmaf(w * w, ru, rr);
+                        }
                     }
                 }
                 buf |= (unsigned long long)bits << nbits;
@@ -722,6 +754,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
             }
         }
         if (keep && nbits) my_hits[wout] = (uint32_t)buf;
+        if (FEAT) write_rates(sc, acc, rr, ti, rate_out);
         write_density(sc, acc, nh, pi, ti, rho_out, p_out, ncount);
     }
     if (lane == 0 && m == M + gridDim.x * (uint32_t)WARPS - 1u) atomicExch(counter, 0u);
@@ -730,18 +763,23 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) density_lane_kernel(
 // ---- force + integration ------------------------------------------------------------------------
 
 // Accumulators of the force pass per target: NF_PLAIN for the step; with FEAT also the time
-// derivative of the pair terms under the pair's relative motion, and the density rate.
-constexpr int NF_PLAIN = 6, NF_FEAT = 13;
+// derivatives of the pair terms.
+constexpr int NF_PLAIN = 6, NF_FEAT = 12;
 
 // One neighbour's pressure and viscosity terms. f[0..2] collects pres*(h-d)^2*r/d and f[3..5]
 // collects (v_j - v_i)*(h-d)/rho_j; the constant factors are applied once per particle.
-// FEAT (the learned rollout's judge steps): with u = v_i - v_j the rate of r, and d' = r.u/d the
-// rate of d, f[6..8] collects d/dt of the pressure term at fixed pressures and densities,
-// (dcoef/dd) d' r + coef u, f[9..11] that of the viscosity term, (v_j - v_i)(-d')/rho_j, and
-// f[12] the Poly6 density rate sum (cull - d2)^2 (r.u) (times -6 m c6 per particle).
+// FEAT (the learned rollout's judge steps): the time derivatives of both, with u = v_i - v_j the
+// rate of r, d' = r.u/d the rate of d and the density pass's rates (rho_j', p_j' in rj, p_i' in
+// pdot_i): f[6..8] collects d/dt of the pressure term,
+//   (dpres/dt (h-d)^2/d + pres d((h-d)^2/d)/dd d') r + coef u,
+//   dpres/dt = (p_i' + p_j') / (2 rho_j) - pres rho_j' / rho_j,
+// and f[9..11] that of the viscosity term without its neighbour-acceleration part,
+//   (v_j - v_i)(-d')/rho_j - (v_j - v_i)(h-d) rho_j' / rho_j^2.
 template <bool FEAT = false>
 __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, const float4& pj, const float4& vj,
-                                           float h, float cull, float* f) {
+                                           float h, float cull, float* f, float pdot_i = 0.f,
+                                           float2 rj = make_float2(0.f, 0.f)) {
+    (void)cull;
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float d2 = dist2(rx, ry, rz);
     const float rsq = d2 > 0.f ? rsqrtf(d2) : 0.f;  // coincident pair (or self): r = 0, no push
@@ -764,40 +802,44 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
         const float ru = fmaf(rz, uz, fmaf(ry, uy, rx * ux));
         const float dp = ru * rsq;  // d'
         if (pres > 0.f) {
-            const float coef = pres * hd * hd * rsq;
+            const float g = hd * hd * rsq;
+            const float coef = pres * g;
+            const float dpres = fmaf(pdot_i + rj.y, 0.5f * inv_rho, -pres * rj.x * inv_rho);
             const float dcoef = -pres * hd * rsq * (2.f + hd * rsq);  // d coef / d d
-            const float cr = dcoef * dp;
+            const float cr = fmaf(dpres, g, dcoef * dp);
             f[6] = fmaf(cr, rx, fmaf(coef, ux, f[6]));
             f[7] = fmaf(cr, ry, fmaf(coef, uy, f[7]));
             f[8] = fmaf(cr, rz, fmaf(coef, uz, f[8]));
         }
-        const float wj = dp * inv_rho;
+        const float wj = inv_rho * fmaf(wv, rj.x, dp);
         f[9] = fmaf(ux, wj, f[9]);
         f[10] = fmaf(uy, wj, f[10]);
         f[11] = fmaf(uz, wj, f[11]);
-        const float w = fmaxf(cull - d2, 0.f);
-        f[12] = fmaf(w * w, ru, f[12]);
     }
 }
 
 // A lane's list (entries list[e * 32 + lane], e < cnt), four entries per round so their loads
 // overlap; an empty place takes the particle itself (slot self), whose terms are exactly zero.
+// FEAT: also the neighbours' rates (rate[k]) and the target's pressure rate pdot_i.
 template <bool FEAT>
 __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t cnt, uint32_t lane, uint32_t self,
                                                 const float4& pi, const float4& vi, const float4* __restrict__ pos,
-                                                const float4* __restrict__ vel, float h, float cull, float* f) {
+                                                const float4* __restrict__ vel, float h, float cull, float* f,
+                                                const float2* __restrict__ rate = nullptr, float pdot_i = 0.f) {
     for (uint32_t e = 0; e < cnt; e += 4u) {
         uint32_t k[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) k[u] = e + (uint32_t)u < cnt ? list[(e + (uint32_t)u) * 32u + lane] : self;
         float4 pj[4], vj[4];
+        float2 rj[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             pj[u] = __ldg(pos + k[u]);
             vj[u] = __ldg(vel + k[u]);
+            rj[u] = FEAT ? __ldg(rate + k[u]) : make_float2(0.f, 0.f);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], h, cull, f);
+        for (int u = 0; u < 4; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], h, cull, f, pdot_i, rj[u]);
     }
 }
 
@@ -808,7 +850,8 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
                                                 const float4& vi, const float* f, uint32_t ti,
                                                 float4* __restrict__ pos_a, float4* __restrict__ vel_a,
                                                 const uint32_t* __restrict__ ids_b, uint32_t* __restrict__ ids_a,
-                                                float4* __restrict__ accel, float4* __restrict__ feat) {
+                                                float4* __restrict__ accel, FeatureBuffers fb = {},
+                                                float rate_i = 0.f) {
     const float fp_scale = -sc.m * sc.cs;         // -m * spiky const
     const float fv_scale = sc.m * sc.cv * sc.mu;  // m * visc const * mu
     const float rho = pi.w, pressure = vi.w;
@@ -852,18 +895,23 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     if (ids_a) ids_a[ti] = ids_b[ti];
     if (accel) accel[ti] = make_float4(acc[0], acc[1], acc[2], 0.f);
     if (FEAT) {
-        // d a / dt under the neighbours' relative motion (pressures and densities held), and the
-        // density rate of the Poly6 sum
+        // J = d a / dt: the pair terms' derivatives over rho_i, and the internal force's share of
+        // d(1/rho_i)/dt = -rho_i' / rho_i^2 (the external terms' derivatives are left out)
         float jk[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) jk[a] = (fp_scale * f[6 + a] + fv_scale * f[9 + a]) * inv;
-        feat[ti] = make_float4(jk[0], jk[1], jk[2], -6.f * sc.m * sc.c6 * f[12]);
+        for (int a = 0; a < 3; ++a) {
+            const float internal = (fp_scale * f[a] + fv_scale * f[3 + a]) * inv;
+            jk[a] = fmaf(-rate_i * inv, internal, (fp_scale * f[6 + a] + fv_scale * f[9 + a]) * inv);
+        }
+        fb.out[ti] = make_float4(jk[0], jk[1], jk[2], rate_i);
     }
 }
 
-// FEAT: the learned rollout's judge step; also writes feat[] (d a/dt, density rate), see pair_terms.
-template <bool BATCHED, bool FEAT = false>
-__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) force_kernel(const SceneConsts sc0, const BatchTables bt,
+// The learned rollout's judge steps use the lane force pass (force_lane_kernel<.., true>); `fb`
+// keeps this kernel's parameters those of the lane kernel (one argument list re-parameterises
+// the captured force node of either variant).
+template <bool BATCHED>
+__global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts sc0, const BatchTables bt,
                                                                const StepInputs in, const uint32_t n,
                                                                const uint32_t num_cells,
                                                                const float4* __restrict__ pos_b,
@@ -877,8 +925,10 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) force_kernel(const 
                                                                const uint32_t* __restrict__ hits,
                                                                float4* __restrict__ accel,
                                                                uint32_t* __restrict__ err,
-                                                               float4* __restrict__ feat = nullptr) {
-    constexpr int NF = FEAT ? NF_FEAT : NF_PLAIN;
+                                                               FeatureBuffers fb = {}) {
+    (void)fb;
+    constexpr bool FEAT = false;
+    constexpr int NF = NF_PLAIN;
     // Per warp: the slot table (candidate number -> sorted slot), then the dense path's per-lane
     // lists and its x/y/z stage; the replay path's neighbour lists use both of those regions.
     __shared__ __align__(16) uint32_t s_work[WARPS][STAGE_CAP + FORCE_REPLAY_LIST];
@@ -1046,7 +1096,7 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) force_kernel(const 
             }
 #pragma unroll
             for (int q = 0; q < NF; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
-            if (tm.sl == 0u) integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, feat);
+            if (tm.sl == 0u) integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
             __syncwarp();  // the slot table is rewritten for the next cell
             continue;
         }
@@ -1132,7 +1182,7 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) force_kernel(const 
             accumulate_list<FEAT>(list, cnt, lane, ti, pi, vi, pos_b, vel_b, sc.h, sc.cull, f);
 #pragma unroll
             for (int q = 0; q < NF; ++q) f[q] = slice_sum(f[q], tm.S, nt, tm.sl);
-            if (tm.sl == 0u) integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, feat);
+            if (tm.sl == 0u) integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel);
         }
         __syncwarp();  // the slot table and stage are rewritten for the next cell
     }
@@ -1163,14 +1213,14 @@ __device__ __forceinline__ uint32_t slot_of(uint32_t q, const uint32_t P[9], con
 }
 
 template <bool BATCHED, bool FEAT = false>
-__global__ void __launch_bounds__(SPH_THREADS, 3) force_lane_kernel(
+__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 2 : 3) force_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const StepInputs in, const uint32_t n, const uint32_t num_cells,
     const float4* __restrict__ pos_b, const float4* __restrict__ vel_b, const uint32_t* __restrict__ ids_b,
     float4* __restrict__ pos_a, float4* __restrict__ vel_a, uint32_t* __restrict__ ids_a,
     const uint32_t* __restrict__ start, const uint32_t* __restrict__ cell_list,
     uint32_t* __restrict__ num_nonempty,  // [2]: this pass's chunk counter
     const uint32_t* __restrict__ hits, float4* __restrict__ accel, uint32_t* __restrict__ err,
-    float4* __restrict__ feat = nullptr) {
+    FeatureBuffers fb = {}) {  // FEAT: the judge step's rates and feature output
     constexpr int NF = FEAT ? NF_FEAT : NF_PLAIN;
     __shared__ uint32_t s_list[WARPS][LANE_LIST * 32];
     __shared__ uint32_t s_poff[BATCHED ? MAX_SCENES + 1 : 1];
@@ -1207,6 +1257,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_lane_kernel(
         const uint32_t* tab = start + coff;
         const float4 pi = pos_b[tself];
         const float4 vi = vel_b[tself];
+        const float2 ri = FEAT ? fb.rate[tself] : make_float2(0.f, 0.f);
         int32_t cx, cy, cz;
         const uint32_t c = bin_key(pi.x, pi.y, pi.z, sc.bin, sc.R, &cx, &cy, &cz);
         const uint32_t cend = min(__ldg(tab + c + 1), n);
@@ -1261,7 +1312,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_lane_kernel(
                 }
             }
             if (!__any_sync(FULL, cnt > 0u)) break;
-            accumulate_list<FEAT>(list, cnt, lane, tself, pi, vi, pos_b, vel_b, sc.h, sc.cull, f);
+            accumulate_list<FEAT>(list, cnt, lane, tself, pi, vi, pos_b, vel_b, sc.h, sc.cull, f, fb.rate, ri.y);
             if (!__any_sync(FULL, more)) break;
         }
         if (live) {
@@ -1271,10 +1322,10 @@ __global__ void __launch_bounds__(SPH_THREADS, 3) force_lane_kernel(
                 vel_a[ti] = vi;
                 if (ids_a) ids_a[ti] = ids_b[ti];
                 if (accel) accel[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (FEAT) feat[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (FEAT) fb.out[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (ti == cbeg && err) atomicOr(err, DEVERR_CELL_OVERFLOW);
             } else {
-                integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, feat);
+                integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, fb, ri.x);
             }
         }
     }
@@ -1288,7 +1339,7 @@ constexpr int arity(void (*)(A...)) {
 }
 // A captured step's force node is re-parameterised from ForceKernelArgs: one pointer per
 // kernel parameter.
-static_assert(arity(&force_kernel<false, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
+static_assert(arity(&force_kernel<false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
 static_assert(arity(&force_lane_kernel<false, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
 static_assert(arity(&force_lane_kernel<true, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
 
@@ -1357,55 +1408,76 @@ void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const La
             reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
 }
 
-// The force pass of variant `ld.pass_variant` (FEAT: the judge steps' feature output too), on a
-// persistent grid sized from that kernel's occupancy.
+// The force pass of variant `ld.pass_variant` on a persistent grid sized from that kernel's
+// occupancy; FEAT (the judge steps): the lane kernel with its feature buffers, on a grid of its
+// own occupancy (more registers per thread than the plain kernel).
 template <bool BATCHED, bool FEAT>
 void launch_force_any(const DevBuffers& d, const SceneConsts& sc, const BatchTables& bt, const StepInputs& in,
-                      const LaunchDims& ld, float4* feat, cudaStream_t s) {
-    const bool lane = ld.pass_variant == PASSES_LANE;
+                      const LaunchDims& ld, FeatureBuffers fb, cudaStream_t s) {
+    const bool lane = FEAT || ld.pass_variant == PASSES_LANE;
     int grid = ld.grid_force;
     if (FEAT) {
-        // more registers per thread than the plain kernel: its own occupancy (cached per variant)
-        static int blocks[2] = {0, 0};
-        int& b = blocks[lane ? 1 : 0];
-        if (!b) {
-            if (lane)
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, force_lane_kernel<BATCHED, true>, SPH_THREADS, 0);
-            else
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, force_kernel<BATCHED, true>, SPH_THREADS, 0);
-            if (b <= 0) b = 1;
+        static int blocks = 0;
+        if (!blocks) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, force_lane_kernel<BATCHED, true>, SPH_THREADS, 0);
+            if (blocks <= 0) blocks = 1;
         }
-        grid = ld.sms * b;
+        grid = ld.sms * blocks;
     }
     if (lane)
         force_lane_kernel<BATCHED, FEAT><<<grid, SPH_THREADS, 0, s>>>(
             sc, bt, in, d.n, d.num_cells, d.pos_b, d.vel_b, d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start, d.cell_list,
-            d.num_nonempty, d.hits, d.accel, d.err, feat);
+            d.num_nonempty, d.hits, d.accel, d.err, fb);
     else
-        force_kernel<BATCHED, FEAT><<<grid, SPH_THREADS, 0, s>>>(sc, bt, in, d.n, d.num_cells, d.pos_b, d.vel_b,
-                                                                d.ids_b, d.pos_a, d.vel_a, d.ids_a, d.start,
-                                                                d.cell_list, d.num_nonempty, d.hits, d.accel, d.err,
-                                                                feat);
+        force_kernel<BATCHED><<<grid, SPH_THREADS, 0, s>>>(sc, bt, in, d.n, d.num_cells, d.pos_b, d.vel_b, d.ids_b,
+                                                          d.pos_a, d.vel_a, d.ids_a, d.start, d.cell_list,
+                                                          d.num_nonempty, d.hits, d.accel, d.err, fb);
 }
 
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s) {
-    launch_force_any<false, false>(d, sc, BatchTables{}, in, ld, nullptr, s);
+    launch_force_any<false, false>(d, sc, BatchTables{}, in, ld, FeatureBuffers{}, s);
 }
 
 void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
                           cudaStream_t s) {
-    launch_force_any<true, false>(d, SceneConsts{}, bt, in, ld, nullptr, s);
+    launch_force_any<true, false>(d, SceneConsts{}, bt, in, ld, FeatureBuffers{}, s);
 }
 
 void launch_force_feat(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
-                       float4* feat, cudaStream_t s) {
-    launch_force_any<false, true>(d, sc, BatchTables{}, in, ld, feat, s);
+                       FeatureBuffers fb, cudaStream_t s) {
+    launch_force_any<false, true>(d, sc, BatchTables{}, in, ld, fb, s);
 }
 
 void launch_force_batched_feat(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
-                               float4* feat, cudaStream_t s) {
-    launch_force_any<true, true>(d, SceneConsts{}, bt, in, ld, feat, s);
+                               FeatureBuffers fb, cudaStream_t s) {
+    launch_force_any<true, true>(d, SceneConsts{}, bt, in, ld, fb, s);
+}
+
+// The judge steps' density pass: the lane kernel with its rate output, on a grid of its own
+// occupancy, whatever ld.pass_variant says (its bit strings are the lane force pass's).
+template <bool BATCHED>
+void launch_density_any_feat(const DevBuffers& d, const SceneConsts& sc, const BatchTables& bt, const LaunchDims& ld,
+                             float2* rate, cudaStream_t s) {
+    static int blocks = 0;
+    if (!blocks) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, density_lane_kernel<BATCHED, true>, SPH_THREADS, 0);
+        if (blocks <= 0) blocks = 1;
+    }
+    uint32_t* nc = BATCHED ? d.ncount : ((sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr);
+    density_lane_kernel<BATCHED, true><<<ld.sms * blocks, SPH_THREADS, 0, s>>>(
+        sc, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3, reinterpret_cast<float*>(d.vel_b) + 3,
+        d.start, d.cell_list, d.num_nonempty, nc, d.hits, d.err, d.vel_b, rate);
+}
+
+void launch_density_feat(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, float2* rate,
+                         cudaStream_t s) {
+    launch_density_any_feat<false>(d, sc, BatchTables{}, ld, rate, s);
+}
+
+void launch_density_batched_feat(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, float2* rate,
+                                 cudaStream_t s) {
+    launch_density_any_feat<true>(d, SceneConsts{}, bt, ld, rate, s);
 }
 
 const void* force_kernel_symbol(int pass_variant) {

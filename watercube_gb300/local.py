@@ -1,7 +1,10 @@
-"""The learned fast rollout over the C ABI (wc_local_*): a per-particle network on the sums of
-the judge step's SPH passes predicts the accelerations of the next K - 1 steps, which then run
-without neighbour passes; every K-th step is plain SPH and judges the last cycle by the carried
-density. No counterpart in the reference, which only runs plain SPH.
+"""The fast rollout over the C ABI (wc_local_*): every K-th step is plain SPH (the judge) and
+also computes each particle's density and pressure rates and the time derivative J of its
+acceleration; the K - 1 steps after it run without neighbour passes on an extrapolated
+acceleration, by mode: the judge's acceleration held (WC_LOCAL_STALE), a + k dt J
+(WC_LOCAL_TAYLOR), or a + k dt J plus a per-particle network's residual (WC_LOCAL_NETWORK). The
+next judge step checks the cycle by the carried density. No counterpart in the reference, which
+only runs plain SPH.
 
 The network, its fused tensor-core inference, training and the rollout are in
 csrc/wc_local.cu; this module moves host arrays and drives training.
@@ -14,7 +17,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _abi as A
-from ._abi import LocalConfig, RolloutStats, check, lib
+from ._abi import WC_LOCAL_NETWORK, WC_LOCAL_STALE, WC_LOCAL_TAYLOR, LocalConfig, RolloutStats, check, lib
 from .batch import Batch
 from .fluid import Fluid
 
@@ -91,15 +94,16 @@ class LocalNet:
         return g, float(loss[0])
 
     def evaluate(self, held_out: bool = True):
-        """(network error, stale error) per age: relative L2 of the acceleration."""
+        """(network, stale, Taylor) errors per age: relative L2 of the acceleration."""
         a = np.zeros(self.ages, np.float32)
         b = np.zeros(self.ages, np.float32)
-        check(lib().wc_local_evaluate(self._h, int(held_out), A._ptr(a), A._ptr(b)), "wc_local_evaluate")
-        return a, b
+        c = np.zeros(self.ages, np.float32)
+        check(lib().wc_local_evaluate(self._h, int(held_out), A._ptr(a), A._ptr(b), A._ptr(c)), "wc_local_evaluate")
+        return a, b, c
 
     def predict(self, fluid: Fluid, dt: float):
-        """(inputs [n, 32], acceleration changes [n, 3 ages]) of the fluid's current state, in the
-        order of the judge step's sort; the fluid does not advance."""
+        """(inputs [n, 32], the network's residuals of the acceleration changes [n, 3 ages]) of the
+        fluid's current state, in the order of the judge step's sort; the fluid does not advance."""
         n = fluid.numParticles()
         x = np.zeros((n, IN), np.float32)
         y = np.zeros((n, 3 * self.ages), np.float32)
@@ -125,13 +129,15 @@ class LocalNet:
 
 
 def rollout(fluid: Fluid, dt: float, nsteps: int, ages: int = 3, tolerance: float = 0.01,
-            net: LocalNet | None = None) -> dict:
-    """Cycles of one judge SPH step and `ages` steps on predicted accelerations (net None: the
-    stale SPH acceleration, the method without the network)."""
+            net: LocalNet | None = None, mode: int | None = None) -> dict:
+    """Cycles of one judge SPH step and `ages` extrapolated steps; mode WC_LOCAL_* (default: the
+    network mode with a net, the stale mode without)."""
     st = RolloutStats()
     h = net._h if net is not None else None
-    check(lib().wc_local_rollout(h, fluid._require(), float(dt), int(nsteps), int(ages), float(tolerance),
-                                 C.byref(st)), "wc_local_rollout")
+    if mode is None:
+        mode = WC_LOCAL_NETWORK if net is not None else WC_LOCAL_STALE
+    check(lib().wc_local_rollout_mode(h, fluid._require(), float(dt), int(nsteps), int(ages), float(tolerance),
+                                      int(mode), C.byref(st)), "wc_local_rollout_mode")
     return st.as_dict()
 
 
