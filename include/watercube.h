@@ -524,9 +524,10 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
  *   WC_LOCAL_STALE    0 (the judge's acceleration held),
  *   WC_LOCAL_TAYLOR   k dt J (first-order extrapolation),
  *   WC_LOCAL_NETWORK  k dt J + the network's residual: a per-particle network maps 19 inputs
- *                     (the SPH acceleration, J dt, the density rate, velocity, density, pressure,
- *                     six wall distances, k / rho0) through two hidden layers of 64 (ReLU) to
- *                     the residuals of ages 1 .. K-1, on the tensor cores (BF16 operands, FP32
+ *                     (the SPH acceleration, J x 1 ms, the density rate, velocity, density,
+ *                     pressure, six wall distances, k / rho0) through two hidden layers of 64
+ *                     (ReLU) to the residuals of ages 1 .. K-1 in units of
+ *                     accel_scale (dt / 1 ms)^2, on the tensor cores (BF16 operands, FP32
  *                     accumulation in tensor memory); their mean over the particles is removed.
  * The skipped steps carry each particle's density by its rate. The judge compares that carried
  * density with the SPH density the next judge step computes for the same particles; a cycle
@@ -568,7 +569,8 @@ WC_API wc_status wc_local_train(wc_local* net, uint32_t steps, uint32_t rows, fl
 WC_API wc_status wc_local_gradients(wc_local* net, const uint32_t* rows_idx, uint32_t rows, float* grads, float* loss);
 /* Copy samples [first, first + count) of a set: inputs [count][32] and targets [count][16]:
    columns 3 (k - 1) .. + 2 the residual (a(t + k) - a(t) - k dt J) / accel_scale of age k,
-   columns 13 .. 15 dt J / accel_scale; either pointer may be NULL. */
+   column 12 (1 ms / dt)^2 (the residuals' factor into the network's units), columns 13 .. 15
+   dt J / accel_scale; either pointer may be NULL. */
 WC_API wc_status wc_local_get_samples(wc_local* net, int held_out, uint64_t first, uint64_t count, float* inputs,
                                       float* targets);
 /* Relative L2 error of the acceleration at each age over a sample set, host [ages] each, as

@@ -108,9 +108,10 @@ def pair_sums(p, sorted_state: np.ndarray, cull: float):
     return acc, jerk, rate
 
 
-def inputs(p, sorted_state: np.ndarray, acc, jerk, rate, dt: float, accel_scale: float = 10.0,
+def inputs(p, sorted_state: np.ndarray, acc, jerk, rate, dt: float = 1e-3, accel_scale: float = 10.0,
            velocity_scale: float = 1.0) -> np.ndarray:
-    """The network's inputs [n, 32] (19 used), float64."""
+    """The network's inputs [n, 32] (19 used), float64; J and the density rate enter times the
+    network's time unit `dt` (1 ms, whatever the solver's time step)."""
     x = sorted_state["position"].astype(np.float64)
     v = sorted_state["velocity"].astype(np.float64)
     rho = sorted_state["density"].astype(np.float64)

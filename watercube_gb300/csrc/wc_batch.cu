@@ -147,7 +147,7 @@ void free_batch(wc_batch* b) {
                     d.unordered, d.perm,         d.counts,     d.start,  d.cell_list,    d.num_nonempty,
                     d.scan_desc, d.scan_tile_counter, d.err,   d.hits,   b->d_scenes,    b->d_poff,
                     b->d_coff,   b->d_diag,      b->staging,   b->flush_buf, b->flush_sink, d.ids_a,
-                    d.ids_b,     d.accel};
+                    d.ids_b,     d.accel,        d.xyz};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->h_err) cudaFreeHost(b->h_err);
@@ -535,6 +535,8 @@ WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, w
     if (st == WC_OK) st = dalloc(&d.ids_a, n);
     if (st == WC_OK) st = dalloc(&d.ids_b, n);
     if (st == WC_OK) st = dalloc(&d.hits, (size_t)n * MASK_WORDS);
+    d.xyz_stride = xyz_stride_for((uint32_t)n);
+    if (st == WC_OK) st = dalloc(&d.xyz, 3 * (size_t)d.xyz_stride);
     if (st == WC_OK) st = dalloc(&d.counts, cells);
     if (st == WC_OK) st = dalloc(&d.start, cells + 1);
     if (st == WC_OK) st = dalloc(&d.cell_list, cells);
@@ -556,6 +558,7 @@ WC_API wc_status wc_batch_create(const wc_params* scenes, uint32_t num_scenes, w
         cudaMemsetAsync(d.num_nonempty, 0, 3 * sizeof(uint32_t), b->stream);
         cudaMemsetAsync(d.start, 0, sizeof(uint32_t) * (cells + 1), b->stream);
         if (n) cudaMemsetAsync(d.hits, 0, sizeof(uint32_t) * MASK_WORDS * (size_t)n, b->stream);
+        cudaMemsetAsync(d.xyz, 0, sizeof(float) * 3 * (size_t)d.xyz_stride, b->stream);
         // the force pass variant of the scenes' flags (a fluid with the same flags gives each scene's
         // result bit for bit)
         const int variant = (b->base[0].flags & WC_FLAG_CELL_TEAMS) ? PASSES_TEAM : PASSES_LANE;

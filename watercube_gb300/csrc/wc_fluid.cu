@@ -63,7 +63,7 @@ void free_all(wc_fluid* f) {
     void* ptrs[] = {d.pos_a,     d.vel_a,        d.pos_b,     d.vel_b,    d.ids_a,           d.ids_b,
                     d.keys,      d.ranks,        d.unordered, d.perm,     d.counts,          d.start,
                     d.cell_list, d.num_nonempty, d.scan_desc, d.ncount,   d.scan_tile_counter, d.err,
-                    d.hits,      f->staging,     f->flush_buf, f->flush_sink, d.accel};
+                    d.hits,      f->staging,     f->flush_buf, f->flush_sink, d.accel,  d.xyz};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (f->h_err) cudaFreeHost(f->h_err);
@@ -93,6 +93,8 @@ wc_status allocate(wc_fluid* f) {
     WC_TRY(dalloc(&d.perm, n));
     if (f->params.flags & WC_FLAG_NEIGHBOR_COUNTS) WC_TRY(dalloc(&d.ncount, n));
     WC_TRY(dalloc(&d.hits, (size_t)n * MASK_WORDS));
+    d.xyz_stride = xyz_stride_for(n);
+    WC_TRY(dalloc(&d.xyz, 3 * (size_t)d.xyz_stride));
     WC_TRY(dalloc(&d.counts, d.num_cells));
     WC_TRY(dalloc(&d.start, (size_t)d.num_cells + 1));
     WC_TRY(dalloc(&d.cell_list, d.num_cells));
@@ -105,6 +107,7 @@ wc_status allocate(wc_fluid* f) {
     WC_CUDA_TRY(cudaMemsetAsync(d.start, 0, sizeof(uint32_t) * ((size_t)d.num_cells + 1), f->stream));
     WC_CUDA_TRY(cudaMemsetAsync(d.num_nonempty, 0, 3 * sizeof(uint32_t), f->stream));
     WC_CUDA_TRY(cudaMemsetAsync(d.err, 0, sizeof(uint32_t), f->stream));
+    WC_CUDA_TRY(cudaMemsetAsync(d.xyz, 0, sizeof(float) * 3 * (size_t)d.xyz_stride, f->stream));
     if (n) {
         WC_CUDA_TRY(cudaMemsetAsync(d.pos_a, 0, sizeof(float4) * n, f->stream));
         WC_CUDA_TRY(cudaMemsetAsync(d.vel_a, 0, sizeof(float4) * n, f->stream));

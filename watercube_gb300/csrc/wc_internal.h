@@ -128,6 +128,9 @@ constexpr int MASK_WORDS = 48;
 // Force kernel dense path: per-lane neighbour list capacity ([CAP][32] words per warp).
 constexpr int FORCE_LIST_CAP = 16;
 
+// The stride of DevBuffers::xyz for n particles.
+inline uint32_t xyz_stride_for(uint32_t n) { return ((n + 3u) & ~3u) + 4u; }
+
 struct DevBuffers {
     uint32_t n;          // particles
     uint32_t num_cells;  // R^3
@@ -147,6 +150,11 @@ struct DevBuffers {
     uint32_t* scan_tile_counter;
     uint32_t* ncount;  // [n] or null
     uint32_t* hits;    // [n * MASK_WORDS] neighbour bit strings
+    // x, y, z of the sorted positions as three float arrays of xyz_stride (a multiple of 4 that
+    // is >= n) elements each, written by the gather for the lane density pass's 16-byte loads of
+    // four consecutive candidates; the padding past n is zero
+    float* xyz;
+    uint32_t xyz_stride;
     float4* accel;     // [n] acceleration of each particle in the last force pass, or null
     uint32_t* err;
 };
@@ -182,22 +190,32 @@ struct FeatureBuffers {
 void launch_bin_count(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
 void launch_scan_cells(const DevBuffers& d, cudaStream_t s);
 void launch_scatter(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s);
-void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s);
+// vxyz (optional, the learned rollout's judge steps): also the sorted velocities' x, y, z as three
+// arrays of d.xyz_stride elements.
+void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s, float* vxyz = nullptr);
 void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, cudaStream_t s);
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s);
+// Feature levels of the judge step's passes: FEAT_RATE (the stale mode's judge) — the density
+// pass's judge sums and the force pass's own density rate; FEAT_FULL (the Taylor and network
+// modes, and sample recording) — also the density and pressure rates from the density pass
+// and the time derivative J of the acceleration from the force pass.
+enum : int { FEAT_NONE = 0, FEAT_RATE = 1, FEAT_FULL = 2 };
+
 // The learned rollout's judge step runs the lane passes with their feature outputs, whatever
-// ld.pass_variant says: the density pass also writes rate[ti] = (density rate, pressure rate),
-// and the force pass reads the neighbours' rates and writes feat[ti] = (J, density rate), J the
-// time derivative of the SPH acceleration (sorted order).
-void launch_density_feat(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, float2* rate,
-                         cudaStream_t s);
-void launch_density_batched_feat(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, float2* rate,
-                                 cudaStream_t s);
+// ld.pass_variant says: the density pass also writes rate[ti] = (density rate, pressure rate)
+// from the gather's velocity arrays vxyz and, when judge_part is given, the judge's sums
+// judge_part[m] = sum over the 32 slots of chunk m of |rho_carried / rho_SPH - 1| (rho_carried:
+// the sorted buffer's .w before the pass); the force pass reads the neighbours' rates and writes
+// feat[ti] = (J, density rate), J the time derivative of the SPH acceleration (sorted order).
+void launch_density_feat(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, int level,
+                         const float* vxyz, float2* rate, float* judge_part, cudaStream_t s);
+void launch_density_batched_feat(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, int level,
+                                 const float* vxyz, float2* rate, float* judge_part, cudaStream_t s);
 void launch_force_feat(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
-                       FeatureBuffers fb, cudaStream_t s);
+                       int level, FeatureBuffers fb, cudaStream_t s);
 void launch_force_batched_feat(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
-                               FeatureBuffers fb, cudaStream_t s);
+                               int level, FeatureBuffers fb, cudaStream_t s);
 // AoS <-> SoA for host copies through a contiguous staging buffer.
 void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, cudaStream_t s);
 void launch_soa_to_aos(const float4* pos, const float4* vel, float4* aos, uint32_t n, cudaStream_t s);

@@ -12,9 +12,13 @@
 // where r_k is a per-particle network's residual of the Taylor term, from 19 inputs of the judge
 // step (with its mean over the particles removed):
 //
-//   x  = [a / a_s, J dt / a_s, 100 rhodot dt / rho, v / v_s, rho / rho0 - 1, p / (k rho0),
+//   x  = [a / a_s, J T / a_s, 100 rhodot T / rho, v / v_s, rho / rho0 - 1, p / (k rho0),
 //         six wall distances / h (clipped to [0, 1]), 100 k / rho0]            (19, padded to 32)
 //   h1 = relu(W1 x + b1) (64),  h2 = relu(W2 h1 + b2) (64),  r = W3 h2 + b3 (16, 3 ages used each)
+//
+// with the network's time unit T = DT_REF = 1 ms; r is in units of a_s (dt / T)^2, the way the
+// residual of a first-order extrapolation scales with the time step, so that the network serves
+// every dt.
 //
 // Inference is one kernel per judge step (mlp_kernel): per 128-particle tile the inputs are
 // computed into shared memory in the tensor cores' K-major core-matrix layout, and the three
@@ -53,6 +57,12 @@ constexpr uint32_t MLP_THREADS = 128;
 constexpr uint32_t MLP_CTAS_PER_SM = 6;
 constexpr uint32_t TMEM_COLS = 64;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
+// The network's time unit: its J and density-rate inputs are J DT_REF / a_s and
+// 100 rhodot DT_REF / rho, and it learns the residual of the Taylor term in units of
+// a_s (dt / DT_REF)^2 (the residual grows with the square of the time step), so that one network
+// serves every dt. Column RES_SCALE of a sample's targets holds (DT_REF / dt)^2.
+constexpr float DT_REF = 1e-3f;
+constexpr uint32_t RES_SCALE = 12;
 
 // FP32 master parameters, W as [k_in x n_out] row-major (the convention of cast_weight).
 constexpr size_t OFF_W1 = 0;
@@ -542,73 +552,45 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
     }
 }
 
-// mean[j] = (sum over CTAs of part[cta][j]) / n, j < OUT: 16 threads per column, FP64, fixed order.
-__global__ void __launch_bounds__(256) output_mean_kernel(uint32_t ctas, uint32_t n, const float* __restrict__ part,
-                                                          float* __restrict__ mean) {
-    __shared__ double s[OUT][16];
-    const uint32_t j = threadIdx.x >> 4, sub = threadIdx.x & 15u;
-    double a = 0.0;
-    for (uint32_t c = sub; c < ctas; c += 16u) a += part[(size_t)c * OUT + j];
-    s[j][sub] = a;
-    __syncthreads();
-    if (sub == 0) {
-        double t = 0.0;
-        for (int q = 0; q < 16; ++q) t += s[j][q];
-        mean[j] = n ? (float)(t / n) : 0.f;
-    }
+// mean[j] = (sum over CTAs of part[cta][j]) / n, j < OUT: one warp per column, FP32 in a fixed
+// order (FP64 arithmetic is slow on this GPU and the mean needs no more than FP32).
+__global__ void __launch_bounds__(32 * OUT) output_mean_kernel(uint32_t ctas, uint32_t n, const float* __restrict__ part,
+                                                               float* __restrict__ mean) {
+    const uint32_t j = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    float a = 0.f;
+    for (uint32_t c = lane; c < ctas; c += 32u) a += part[(size_t)c * OUT + j];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+    if (lane == 0) mean[j] = n ? a / (float)n : 0.f;
 }
 
 // ---- rollout kernels ----------------------------------------------------------------------------
 
-// dst[i] = src[i].w
-__global__ void copy_w_kernel(uint32_t n, const float4* __restrict__ src, float* __restrict__ dst) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = src[i].w;
-}
-
-// Judge: per-block sums (FP64) of |carried / rho_SPH - 1| over the sorted buffer after the
-// density pass, then one fixed-order sum of the block sums.
-constexpr uint32_t JUDGE_THREADS = 256;
-constexpr uint32_t JUDGE_BLOCKS = 512;
-__global__ void __launch_bounds__(JUDGE_THREADS) judge_partial_kernel(uint32_t n, const float* __restrict__ carried,
-                                                                      const float4* __restrict__ pos_b,
-                                                                      double* __restrict__ part) {
-    __shared__ double s[JUDGE_THREADS / 32];
-    // the ratio in FP32 (relative rounding 1e-7 against a tolerance of order 1e-2); a thread's
-    // few terms and a warp's sum in FP32, the rest in FP64, every sum in a fixed order
-    float e = 0.f;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float r = pos_b[i].w;
-        const float q = r != 0.f ? fabsf(__fdividef(carried[i], r) - 1.f) : 0.f;
-        e += isfinite(q) ? q : 1.f;
-    }
+// Judge: the judge step's density pass sums |rho_carried / rho_SPH - 1| per chunk of 32 sorted
+// slots; this kernel adds the chunk sums in a fixed order, FP32 per thread and warp (a relative
+// rounding of order 1e-6 against a tolerance of order 1e-2), FP64 across the warps.
+constexpr uint32_t JUDGE_THREADS = 1024;
+__global__ void __launch_bounds__(JUDGE_THREADS) judge_final_kernel(uint32_t chunks, const float* __restrict__ part,
+                                                                    double* __restrict__ out) {
+    __shared__ float s[JUDGE_THREADS / 32];
+    float a = 0.f;
+    for (uint32_t b = threadIdx.x; b < chunks; b += JUDGE_THREADS) a += part[b];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) e += __shfl_xor_sync(0xffffffffu, e, off);
-    if ((threadIdx.x & 31u) == 0) s[threadIdx.x >> 5] = e;
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+    if ((threadIdx.x & 31u) == 0) s[threadIdx.x >> 5] = a;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0;
-        for (uint32_t w = 0; w < JUDGE_THREADS / 32; ++w) a += s[w];
-        part[blockIdx.x] = a;
+        double t = 0.0;
+        for (uint32_t w = 0; w < JUDGE_THREADS / 32; ++w) t += s[w];
+        *out = t;
     }
-}
-__global__ void judge_final_kernel(uint32_t blocks, const double* __restrict__ part, double* __restrict__ out) {
-    __shared__ double s[256];
-    double a = 0.0;
-    for (uint32_t b = threadIdx.x; b < blocks; b += 256) a += part[b];
-    s[threadIdx.x] = a;
-    __syncthreads();
-    for (uint32_t h = 128; h > 0; h >>= 1) {
-        if (threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *out = s[0];
 }
 
 // ---- sample recording ---------------------------------------------------------------------------
 
 // a0_by_id[ids[i]] = acc[i]
-// The judge step's acceleration and J by particle id; y_by_id[id][13 .. 15] = dt J / a_s.
+// The judge step's acceleration and J by particle id; y_by_id[id][13 .. 15] = dt J / a_s and
+// y_by_id[id][RES_SCALE] = (DT_REF / dt)^2.
 __global__ void scatter_judge_kernel(uint32_t n, const uint32_t* __restrict__ ids, const float4* __restrict__ acc,
                                      const float4* __restrict__ feat, float dt, float inv_a,
                                      float4* __restrict__ a0_by_id, float4* __restrict__ j0_by_id,
@@ -620,6 +602,7 @@ __global__ void scatter_judge_kernel(uint32_t n, const uint32_t* __restrict__ id
     a0_by_id[id] = acc[i];
     j0_by_id[id] = j;
     float* y = y_by_id + (size_t)id * OUT;
+    y[RES_SCALE] = (DT_REF / dt) * (DT_REF / dt);
     y[13] = j.x * dt * inv_a;
     y[14] = j.y * dt * inv_a;
     y[15] = j.z * dt * inv_a;
@@ -665,10 +648,12 @@ __global__ void gather_rows_kernel(uint32_t rows, uint64_t seed, uint64_t count,
     uint4* dx = reinterpret_cast<uint4*>(xb + (size_t)r * IN);
 #pragma unroll
     for (int q = 0; q < (int)IN / 8; ++q) dx[q] = sx[q];
-    const float4* sy = reinterpret_cast<const float4*>(ys + k * OUT);
-    float4* dy = reinterpret_cast<float4*>(yb + (size_t)r * OUT);
+    // the residuals in the network's units: times (DT_REF / dt)^2 (column RES_SCALE)
+    const float* sy = ys + k * OUT;
+    const float sc = sy[RES_SCALE];
+    float* dy = yb + (size_t)r * OUT;
 #pragma unroll
-    for (int q = 0; q < (int)OUT / 4; ++q) dy[q] = sy[q];
+    for (int q = 0; q < (int)OUT; ++q) dy[q] = q < (int)RES_SCALE ? sy[q] * sc : 0.f;
 }
 
 // Mean squared error over the used outputs: d = 2 (p - t) / (rows nout) (FP32 and BF16, unused
@@ -713,7 +698,8 @@ __global__ void reduce_splits_kernel(uint32_t count, uint32_t splits, const floa
 }
 
 // Evaluation sums per age k (units of a_s; y the residual, jd = dt J from the targets' columns
-// 13 .. 15, a0 from the inputs' first three columns): |pred - y|^2 (network mode),
+// 13 .. 15, a0 from the inputs' first three columns, pred converted from the network's units):
+// |pred - y|^2 (network mode),
 // |y + k jd|^2 (stale mode), |y|^2 (Taylor mode), |a0 + y + k jd|^2 (the acceleration).
 constexpr uint32_t EVAL_SUMS = 4;
 __global__ void eval_kernel(uint64_t rows, uint32_t ages, const __nv_bfloat16* __restrict__ xs,
@@ -730,7 +716,7 @@ __global__ void eval_kernel(uint64_t rows, uint32_t ages, const __nv_bfloat16* _
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const double y = ys[r * OUT + 3 * g + c];
-                const double p = pred[r * OUT + 3 * g + c];
+                const double p = pred[r * OUT + 3 * g + c] / (double)ys[r * OUT + RES_SCALE];
                 const double ch = y + (double)(g + 1) * ys[r * OUT + 13 + c];
                 const double t = a0[c] + ch;
                 acc[EVAL_SUMS * g + 0] += (p - y) * (p - y);
@@ -787,10 +773,11 @@ struct wc_local {
     float* change = nullptr;
     float* mean_part = nullptr;  // per-CTA column sums of the network's outputs
     float* mean = nullptr;       // their mean over the particles [OUT]
-    float* carried = nullptr;
+    float* vxyz = nullptr;  // judge steps: the gather's sorted velocities (x, y, z arrays)
     float4 *save_pos[2] = {nullptr, nullptr}, *save_vel[2] = {nullptr, nullptr};
     uint32_t* save_ids[2] = {nullptr, nullptr};
-    double *judge_part = nullptr, *judge_out = nullptr, *h_judge = nullptr;
+    float* judge_part = nullptr;  // per chunk of 32 sorted slots
+    double *judge_out = nullptr, *h_judge = nullptr;
     uint32_t cap_roll = 0;
 };
 
@@ -831,7 +818,7 @@ void free_local(wc_local* s) {
     dfree(s->change);
     dfree(s->mean_part);
     dfree(s->mean);
-    dfree(s->carried);
+    dfree(s->vxyz);
     dfree(s->judge_part);
     dfree(s->judge_out);
     if (s->h_err) cudaFreeHost(s->h_err);
@@ -881,9 +868,13 @@ InputSrc input_src(const wc_local* s, const StepTarget& t, float dt) {
     src.feat = s->feat;
     src.sc = t.sc;
     src.bt = t.bt;
-    src.fs = FeatureScales{1.f / s->cfg.accel_scale, 1.f / s->cfg.velocity_scale, dt};
+    (void)dt;
+    src.fs = FeatureScales{1.f / s->cfg.accel_scale, 1.f / s->cfg.velocity_scale, DT_REF};
     return src;
 }
+
+// The network's outputs -> m/s^2 at time step dt: a_s (dt / DT_REF)^2.
+float residual_scale(const wc_local* s, float dt) { return s->cfg.accel_scale * (dt / DT_REF) * (dt / DT_REF); }
 
 // The network on the judge step's buffers -> s->change [n x 4 ages] (accelerations, m/s^2).
 void enqueue_predict(wc_local* s, const StepTarget& t, float dt) {
@@ -894,14 +885,15 @@ void enqueue_predict(wc_local* s, const StepTarget& t, float dt) {
     const uint32_t ldo = 3u * s->cfg.ages;
     if (t.bt.num_scenes)
         mlp_kernel<true, true><<<mlp_grid(s, n), MLP_THREADS, 0, s->stream>>>(
-            n, src, nullptr, weights(s), s->change, ldo, ldo, s->cfg.accel_scale, s->d_err);
+            n, src, nullptr, weights(s), s->change, ldo, ldo, residual_scale(s, dt), s->d_err);
     else
         mlp_kernel<true, false><<<mlp_grid(s, n), MLP_THREADS, 0, s->stream>>>(
-            n, src, nullptr, weights(s), s->change, ldo, ldo, s->cfg.accel_scale, s->d_err);
+            n, src, nullptr, weights(s), s->change, ldo, ldo, residual_scale(s, dt), s->d_err);
 }
 
-// The judge of the last cycle when the rollout ends after its skipped steps: the sort, the
-// carried densities and the density pass, without a force pass (the state does not advance).
+// The judge of the last cycle when the rollout ends after its skipped steps: the sort and the
+// judge step's density pass with its judge sums, without a force pass (the state does not
+// advance).
 void enqueue_closing_judge(wc_local* s, const StepTarget& t) {
     DevBuffers& d = *t.d;
     if (!d.n) return;
@@ -912,21 +904,19 @@ void enqueue_closing_judge(wc_local* s, const StepTarget& t) {
     launch_scan_cells(d, t.stream);
     launch_scatter(d, t.ld, t.stream);
     launch_rank_gather(d, t.ld, t.stream);
-    copy_w_kernel<<<blocks_for(d.n, 256), 256, 0, t.stream>>>(d.n, d.pos_b, s->carried);
     if (t.bt.num_scenes)
-        launch_density_batched(d, t.bt, t.ld, t.stream);
+        launch_density_batched_feat(d, t.bt, t.ld, FEAT_RATE, nullptr, nullptr, s->judge_part, t.stream);
     else
-        launch_density(d, t.sc, t.ld, t.stream);
-    const uint32_t blocks = std::min(blocks_for(d.n, JUDGE_THREADS), JUDGE_BLOCKS);
-    judge_partial_kernel<<<blocks, JUDGE_THREADS, 0, t.stream>>>(d.n, s->carried, d.pos_b, s->judge_part);
-    judge_final_kernel<<<1, 256, 0, t.stream>>>(blocks, s->judge_part, s->judge_out);
+        launch_density_feat(d, t.sc, t.ld, FEAT_RATE, nullptr, nullptr, s->judge_part, t.stream);
+    judge_final_kernel<<<1, JUDGE_THREADS, 0, t.stream>>>(blocks_for(d.n, 32), s->judge_part, s->judge_out);
 }
 
-// The judge step (a plain SPH step whose density pass also writes s->rate and whose force pass
-// also writes s->feat), on the target's stream.
-// When `carried` is set, the sorted buffer's densities before the density pass (the carried
-// ones) are kept there and the judge sums are enqueued after it.
-void enqueue_judge_step(wc_local* s, const StepTarget& t, float dt, bool judge) {
+// The judge step, on the target's stream: a plain SPH step whose force pass also writes s->feat
+// (feature level FEAT_RATE: the density rate in .w; FEAT_FULL: also J, from the density pass's
+// rates in s->rate). With `judge`, the density pass also sums |rho_carried / rho_SPH - 1| (the
+// sorted buffer's densities before the pass are the ones the skipped steps carried) and the final
+// sum follows it.
+void enqueue_judge_step(wc_local* s, const StepTarget& t, float dt, bool judge, int level = FEAT_FULL) {
     DevBuffers& d = *t.d;
     StepInputs in = *t.in;
     in.dt = dt;
@@ -937,21 +927,18 @@ void enqueue_judge_step(wc_local* s, const StepTarget& t, float dt, bool judge) 
     }
     launch_scan_cells(d, t.stream);
     launch_scatter(d, t.ld, t.stream);
-    launch_rank_gather(d, t.ld, t.stream);
-    if (judge && d.n) copy_w_kernel<<<blocks_for(d.n, 256), 256, 0, t.stream>>>(d.n, d.pos_b, s->carried);
+    const bool full = level == FEAT_FULL;
+    launch_rank_gather(d, t.ld, t.stream, full ? s->vxyz : nullptr);
     const FeatureBuffers fb{s->feat, s->rate};
+    float* jp = judge && d.n ? s->judge_part : nullptr;
     if (t.bt.num_scenes) {
-        launch_density_batched_feat(d, t.bt, t.ld, s->rate, t.stream);
-        launch_force_batched_feat(d, t.bt, in, t.ld, fb, t.stream);
+        launch_density_batched_feat(d, t.bt, t.ld, level, s->vxyz, s->rate, jp, t.stream);
+        launch_force_batched_feat(d, t.bt, in, t.ld, level, fb, t.stream);
     } else {
-        launch_density_feat(d, t.sc, t.ld, s->rate, t.stream);
-        launch_force_feat(d, t.sc, in, t.ld, fb, t.stream);
+        launch_density_feat(d, t.sc, t.ld, level, s->vxyz, s->rate, jp, t.stream);
+        launch_force_feat(d, t.sc, in, t.ld, level, fb, t.stream);
     }
-    if (judge && d.n) {
-        const uint32_t blocks = std::min(blocks_for(d.n, JUDGE_THREADS), JUDGE_BLOCKS);
-        judge_partial_kernel<<<blocks, JUDGE_THREADS, 0, t.stream>>>(d.n, s->carried, d.pos_b, s->judge_part);
-        judge_final_kernel<<<1, 256, 0, t.stream>>>(blocks, s->judge_part, s->judge_out);
-    }
+    if (jp) judge_final_kernel<<<1, JUDGE_THREADS, 0, t.stream>>>(blocks_for(d.n, 32), jp, s->judge_out);
 }
 
 wc_status plain_step(const StepTarget& t, float dt) {
@@ -972,6 +959,7 @@ wc_status ensure_n(wc_local* s, uint32_t n) {
     dfree(s->j0_id);
     dfree(s->feat);
     dfree(s->rate);
+    dfree(s->vxyz);
     s->cap_n = 0;
     WC_TRY(dalloc(&s->x_id, (size_t)n * IN));
     WC_TRY(dalloc(&s->y_id, (size_t)n * OUT));
@@ -979,6 +967,7 @@ wc_status ensure_n(wc_local* s, uint32_t n) {
     WC_TRY(dalloc(&s->j0_id, n));
     WC_TRY(dalloc(&s->feat, n));
     WC_TRY(dalloc(&s->rate, n));
+    WC_TRY(dalloc(&s->vxyz, 3 * (size_t)xyz_stride_for(n)));
     s->cap_n = n;
     return WC_OK;
 }
@@ -1004,7 +993,7 @@ wc_status record(wc_local* s, const StepTarget& t0, float dt, uint32_t cycles, i
     if (!had_accel) WC_TRY(set_recording(t, true));
     t.ld = t0.fluid ? fluid_target(t0.fluid).ld : batch_target(t0.batch).ld;
     const uint32_t ages = s->cfg.ages;
-    const FeatureScales fs{1.f / s->cfg.accel_scale, 1.f / s->cfg.velocity_scale, dt};
+    const FeatureScales fs{1.f / s->cfg.accel_scale, 1.f / s->cfg.velocity_scale, DT_REF};
     wc_status rc = WC_OK;
     for (uint32_t c = 0; c < cycles && rc == WC_OK; ++c) {
         if (s->count[set] + n > s->cap[set]) break;  // full
@@ -1201,7 +1190,6 @@ wc_status ensure_roll(wc_local* s, uint32_t n) {
     dfree(s->change);
     dfree(s->mean_part);
     dfree(s->mean);
-    dfree(s->carried);
     dfree(s->judge_part);
     for (int q = 0; q < 2; ++q) {
         dfree(s->save_pos[q]);
@@ -1212,8 +1200,7 @@ wc_status ensure_roll(wc_local* s, uint32_t n) {
     WC_TRY(dalloc(&s->change, (size_t)n * 3u * MAX_AGES));
     if (!s->mean_part) WC_TRY(dalloc(&s->mean_part, (size_t)s->sms * MLP_CTAS_PER_SM * OUT));
     if (!s->mean) WC_TRY(dalloc(&s->mean, OUT));
-    WC_TRY(dalloc(&s->carried, n));
-    WC_TRY(dalloc(&s->judge_part, blocks_for(n, JUDGE_THREADS)));
+    WC_TRY(dalloc(&s->judge_part, blocks_for(n, 32)));
     for (int q = 0; q < 2; ++q) {
         WC_TRY(dalloc(&s->save_pos[q], n));
         WC_TRY(dalloc(&s->save_vel[q], n));
@@ -1508,6 +1495,8 @@ WC_API wc_status wc_local_rollout_mode(wc_local* s, wc_fluid* f, float dt, uint3
         return fail(WC_ERR_INVALID_ARG, "the network predicts %u ages", s->cfg.ages);
     wc_local* const net = mode == WC_LOCAL_NETWORK ? s : nullptr;
     const uint32_t taylor = mode != WC_LOCAL_STALE ? 1u : 0u;
+    // the stale mode's judge steps need only the density rate (carried densities), not J
+    const int level = mode == WC_LOCAL_STALE ? FEAT_RATE : FEAT_FULL;
     std::memset(out, 0, sizeof *out);
     // a rollout without a network handle still needs the judge's scratch: a private one
     wc_local* own = nullptr;
@@ -1562,9 +1551,9 @@ WC_API wc_status wc_local_rollout_mode(wc_local* s, wc_fluid* f, float dt, uint3
             const InputSrc src = input_src(net, t, dt);
             const int grid = mlp_grid(net, n);
             mlp_kernel<true, false, true><<<grid, MLP_THREADS, 0, t.stream>>>(
-                n, src, nullptr, weights(net), w->change, 3u * MAX_AGES, 3u * MAX_AGES, net->cfg.accel_scale, net->d_err,
+                n, src, nullptr, weights(net), w->change, 3u * MAX_AGES, 3u * MAX_AGES, residual_scale(net, dt), net->d_err,
                 w->mean_part);  // all 3 MAX_AGES columns (whole 16-byte stores); the skipped steps read 3 count
-            output_mean_kernel<<<1, 256, 0, t.stream>>>((uint32_t)grid, n, w->mean_part, w->mean);
+            output_mean_kernel<<<1, 32 * OUT, 0, t.stream>>>((uint32_t)grid, n, w->mean_part, w->mean);
             skip_cycle_kernel<false><<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.sc, BatchTables{}, k, w->change,
                                                                                3u * MAX_AGES, w->mean);
         } else {
@@ -1575,7 +1564,7 @@ WC_API wc_status wc_local_rollout_mode(wc_local* s, wc_fluid* f, float dt, uint3
     uint32_t last_skip = 0;  // skipped steps of the last cycle (judged at the end when > 0)
     while (rc == WC_OK && done < nsteps) {
         const uint32_t skip = std::min(ages, nsteps - done - 1u);
-        enqueue_judge_step(w, t, dt, have_prev);
+        enqueue_judge_step(w, t, dt, have_prev, level);
         if (have_prev) {
             cudaMemcpyAsync(w->h_judge, w->judge_out, sizeof(double), cudaMemcpyDeviceToHost, t.stream);
             cudaEventRecord(ej, t.stream);
@@ -1599,7 +1588,7 @@ WC_API wc_status wc_local_rollout_mode(wc_local* s, wc_fluid* f, float dt, uint3
                 for (uint32_t k = 0; k < last_skip && rc == WC_OK; ++k) rc = fluid_graph_step(f, dt);
                 out->surrogate_steps -= last_skip;
                 out->sph_steps += last_skip;
-                enqueue_judge_step(w, t, dt, false);
+                enqueue_judge_step(w, t, dt, false, level);
                 skip_steps(skip, cur);
             }
         }

@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(256) rank_gather_kernel(uint32_t n, const uint
                                                           const uint32_t* __restrict__ ids_in,
                                                           float4* __restrict__ pos_out, float4* __restrict__ vel_out,
                                                           uint32_t* __restrict__ ids_out, uint32_t* __restrict__ perm,
-                                                          uint32_t* __restrict__ err) {
+                                                          uint32_t* __restrict__ err, float* __restrict__ xyz,
+                                                          uint32_t xyz_stride, float* __restrict__ vxyz) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t key = keys[i];
         const uint32_t s = start[key], e = min(start[key + 1], n);
@@ -284,7 +285,19 @@ __global__ void __launch_bounds__(256) rank_gather_kernel(uint32_t n, const uint
         const uint32_t dst = s + r;
         if (dst >= n) continue;
         perm[dst] = i;
-        pos_out[dst] = pos_in[i];
+        const float4 p = pos_in[i];
+        pos_out[dst] = p;
+        if (xyz) {
+            xyz[dst] = p.x;
+            xyz[xyz_stride + dst] = p.y;
+            xyz[2 * (size_t)xyz_stride + dst] = p.z;
+        }
+        if (VEL && vxyz) {
+            const float4 v = vel_in[i];
+            vxyz[dst] = v.x;
+            vxyz[xyz_stride + dst] = v.y;
+            vxyz[2 * (size_t)xyz_stride + dst] = v.z;
+        }
         if (VEL) vel_out[dst] = vel_in[i];
         if (IDS) ids_out[dst] = ids_in[i];
     }
@@ -349,17 +362,20 @@ void launch_scatter(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s) {
     scatter_cells_kernel<<<grid_for(d.n, ld.grid_stream), 256, 0, s>>>(d.n, d.keys, d.ranks, d.start, d.unordered);
 }
 
-void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s) {
+void launch_rank_gather(const DevBuffers& d, const LaunchDims& ld, cudaStream_t s, float* vxyz) {
     const int g = grid_for(d.n, ld.grid_stream);
     if (!d.vel_a)
         rank_gather_kernel<false, false><<<g, 256, 0, s>>>(d.n, d.keys, d.ranks, d.unordered, d.start, d.pos_a, nullptr,
-                                                           nullptr, d.pos_b, nullptr, nullptr, d.perm, d.err);
+                                                           nullptr, d.pos_b, nullptr, nullptr, d.perm, d.err, d.xyz,
+                                                           d.xyz_stride, nullptr);
     else if (d.ids_a)
         rank_gather_kernel<true, true><<<g, 256, 0, s>>>(d.n, d.keys, d.ranks, d.unordered, d.start, d.pos_a, d.vel_a,
-                                                         d.ids_a, d.pos_b, d.vel_b, d.ids_b, d.perm, d.err);
+                                                         d.ids_a, d.pos_b, d.vel_b, d.ids_b, d.perm, d.err, d.xyz,
+                                                         d.xyz_stride, vxyz);
     else
         rank_gather_kernel<false, true><<<g, 256, 0, s>>>(d.n, d.keys, d.ranks, d.unordered, d.start, d.pos_a,
-                                                          d.vel_a, nullptr, d.pos_b, d.vel_b, nullptr, d.perm, d.err);
+                                                          d.vel_a, nullptr, d.pos_b, d.vel_b, nullptr, d.perm, d.err,
+                                                          d.xyz, d.xyz_stride, vxyz);
 }
 
 void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, cudaStream_t s) {

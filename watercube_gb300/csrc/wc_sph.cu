@@ -382,8 +382,8 @@ __device__ __forceinline__ void wall_weight_push(const SceneConsts& c, const flo
     }
 }
 
-__device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, uint32_t hits, const float4& pi,
-                                              uint32_t ti, float* rho_out, float* p_out, uint32_t* ncount) {
+__device__ __forceinline__ float write_density(const SceneConsts& sc, float sum, uint32_t hits, const float4& pi,
+                                               uint32_t ti, float* rho_out, float* p_out, uint32_t* ncount) {
     // The sum includes the particle itself (w = h^2): the reference's m*W(0) term.
     float rho = (sc.m * sc.c6) * sum;
     if (sc.flags & WC_FLAG_WALL_WEIGHTS) rho += wall_weight_density(sc, pi.x, pi.y, pi.z);
@@ -399,6 +399,7 @@ __device__ __forceinline__ void write_density(const SceneConsts& sc, float sum, 
     rho_out[4 * (size_t)ti] = total;
     p_out[4 * (size_t)ti] = pressure;
     if (ncount) ncount[ti] = hits - 1u;
+    return total;
 }
 
 // The judge step's rates of one particle from its density-pass sums: the Poly6 density rate
@@ -625,7 +626,10 @@ __global__ void __launch_bounds__(SPH_THREADS, 5) density_kernel(const SceneCons
 // its own candidate numbering (bit b of word w: candidate 32 w + b of the rows concatenated),
 // kept when it fits the slot (at most 32 MASK_WORDS candidates); the lane force pass reads it.
 // FEAT (the learned rollout's judge steps): each hit also adds (cull - d2)^2 (r . u), u = v_i - v_j,
-// to the Poly6 density rate, and the pass writes rate_out[ti] = (density rate, pressure rate).
+// to the Poly6 density rate (the candidates' velocities from the gather's arrays vxyz, four at a
+// time like the positions), and the pass writes rate_out[ti] = (density rate, pressure rate);
+// with judge_part it also sums |rho_carried / rho - 1| over each chunk of 32 slots into
+// judge_part[m] (rho_carried: the slot's .w before this pass; a non-finite ratio counts 1).
 
 // Rows of the 27 neighbour cells of cell (cx, cy, cz): P[r] = first candidate of row r in the
 // concatenated numbering, D[r] = first slot of row r - P[r]; returns the candidate total.
@@ -650,15 +654,17 @@ __device__ __forceinline__ uint32_t lane_rows(const uint32_t* __restrict__ tab, 
     return total;
 }
 
-template <bool BATCHED, bool FEAT = false>
-__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) density_lane_kernel(
+template <bool BATCHED, int FEAT = FEAT_NONE>
+__global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 3 : 4) density_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const uint32_t n, const uint32_t num_cells,
     const float4* pos_in,  // its .w lanes are the density output: read with coherent loads
     float* rho_out, float* p_out, const uint32_t* __restrict__ start, const uint32_t* __restrict__ cell_list,
     uint32_t* __restrict__ num_nonempty,  // [1]: this pass's chunk counter
     uint32_t* __restrict__ ncount, uint32_t* __restrict__ hits, uint32_t* __restrict__ err,
+    const float* __restrict__ xyz, const uint32_t xyz_stride,  // the gather's x, y, z arrays
     const float4* vel_in = nullptr,  // FEAT: velocities (their .w lanes are the pressure output)
-    float2* __restrict__ rate_out = nullptr) {
+    const float* __restrict__ vxyz = nullptr, float2* __restrict__ rate_out = nullptr,
+    float* __restrict__ judge_part = nullptr) {
     __shared__ uint32_t s_poff[BATCHED ? MAX_SCENES + 1 : 1];
     __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
     if (BATCHED) {
@@ -678,7 +684,9 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) density_lane_kernel
     for (; m < M; m = __shfl_sync(FULL, m_next, 0)) {
         if (lane == 0) m_next = atomicAdd(counter, 1u);
         const uint32_t ti = (m << 5) + lane;
-        if (ti >= n) continue;
+        float judge = 0.f;  // FEAT with judge_part: this slot's |rho_carried / rho - 1|
+        do {
+        if (ti >= n) break;
         SceneConsts sc;
         uint32_t coff = 0;
         if (BATCHED) {
@@ -699,17 +707,28 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) density_lane_kernel
             rho_out[4 * (size_t)ti] = __int_as_float(0x7fc00000);
             p_out[4 * (size_t)ti] = __int_as_float(0x7fc00000);
             if (ncount) ncount[ti] = 0u;
-            if (FEAT) rate_out[ti] = make_float2(0.f, 0.f);
+            if (FEAT == FEAT_FULL) rate_out[ti] = make_float2(0.f, 0.f);
             if (ti == cbeg && err) atomicOr(err, DEVERR_CELL_OVERFLOW);
-            continue;
+            judge = 1.f;
+            break;
         }
         uint32_t P[9], D[9];
         const uint32_t total = lane_rows(tab, n, sc.R, cx, cy, cz, P, D);
         const bool keep = hits != nullptr && total <= 32u * (uint32_t)MASK_WORDS;
         uint32_t* my_hits = hits ? hits + (size_t)ti * MASK_WORDS : nullptr;
         float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (FEAT) vi = vel_in[ti];
+        if (FEAT == FEAT_FULL) vi = vel_in[ti];
         float rr = 0.f;  // FEAT: sum of (cull - d2)^2 (r . u)
+        const float* X = xyz;
+        const float* Y = xyz + xyz_stride;
+        const float* Z = xyz + 2 * (size_t)xyz_stride;
+        const float* VX = vxyz;
+        const float* VY = vxyz + xyz_stride;
+        const float* VZ = vxyz + 2 * (size_t)xyz_stride;
+        const f2 px = pk(pi.x, pi.x), py = pk(pi.y, pi.y), pz = pk(pi.z, pi.z), cull2 = pk(sc.cull, sc.cull);
+        const f2 pvx = pk(vi.x, vi.x), pvy = pk(vi.y, vi.y), pvz = pk(vi.z, vi.z);
+        // the weights are added one by one in candidate order, so that the sum does not depend on
+        // where the quads fall (a scene of a batch sees the same sums as the scene alone)
         float acc = 0.f;
         uint32_t nh = 0, nbits = 0, wout = 0;
         unsigned long long buf = 0ull;  // hit bits not yet stored, candidate order
@@ -717,34 +736,56 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) density_lane_kernel
         for (int r = 0; r < 9; ++r) {
             const uint32_t lo = P[r] + D[r];
             const uint32_t end = lo + ((r < 8 ? P[r + 1] : total) - P[r]);
-            // four candidates per round, their loads in flight together (a short round re-reads
-            // the row's last candidate and ignores it)
-            for (uint32_t k = lo; k < end; k += 4u) {
-                const uint32_t cnt = min(4u, end - k);
-                float4 pj[4];
-#pragma unroll
-                for (uint32_t u = 0; u < 4u; ++u) pj[u] = pos_in[min(k + u, end - 1u)];
-                uint32_t bits = 0;
-#pragma unroll
-                for (uint32_t u = 0; u < 4u; ++u) {
-                    const float d2 = dist2(pi.x - pj[u].x, pi.y - pj[u].y, pi.z - pj[u].z);
-                    // d2 <= cull is the reference's sqrtf(d2) < h; the weight (cull - d2)^3 is
-                    // Poly6's (h^2 - r^2)^3 with h^2 to the ulp (the target itself: r = 0)
-                    const float w = sc.cull - d2;
-                    if (u < cnt && w >= 0.f) {
-                        acc = fmaf(w * w, w, acc);
-                        ++nh;
-                        bits |= 1u << u;
-                        if (FEAT) {
-                            const float4 vj = vel_in[k + u];
-                            const float ru = fmaf(pi.z - pj[u].z, vi.z - vj.z,
-                                                  fmaf(pi.y - pj[u].y, vi.y - vj.y, (pi.x - pj[u].x) * (vi.x - vj.x)));
-                            rr = fmaf(w * w, ru, rr);
-                        }
-                    }
+            // the aligned quads of the x, y, z arrays that cover [lo, end), one 16-byte load per
+            // coordinate and the packed f32x2 test (the same fused operations per element as the
+            // scalar test); quad places outside the row are masked out
+            for (uint32_t k = lo & ~3u; k < end; k += 4u) {
+                const ulonglong2 qx = *reinterpret_cast<const ulonglong2*>(X + k);
+                const ulonglong2 qy = *reinterpret_cast<const ulonglong2*>(Y + k);
+                const ulonglong2 qz = *reinterpret_cast<const ulonglong2*>(Z + k);
+                const f2 dx01 = sub2(px, qx.x), dx23 = sub2(px, qx.y);
+                const f2 dy01 = sub2(py, qy.x), dy23 = sub2(py, qy.y);
+                const f2 dz01 = sub2(pz, qz.x), dz23 = sub2(pz, qz.y);
+                const f2 d01 = fma2(dz01, dz01, fma2(dy01, dy01, mul2(dx01, dx01)));
+                const f2 d23 = fma2(dz23, dz23, fma2(dy23, dy23, mul2(dx23, dx23)));
+                // w = cull - d2 >= 0 exactly when d2 <= cull (the reference's sqrtf(d2) < h; a tie
+                // gives +0), and (cull - d2)^3 is Poly6's (h^2 - r^2)^3 with h^2 to the ulp
+                float w0, w1, w2, w3;
+                upk(sub2(cull2, d01), w0, w1);
+                upk(sub2(cull2, d23), w2, w3);
+                const uint32_t s0 = lo > k ? lo - k : 0u;
+                const uint32_t e0 = min(end - k, 4u);
+                const uint32_t valid = (0xFu >> (4u - e0)) & (0xFu << s0);
+                const uint32_t miss = (__float_as_uint(w0) >> 31) | ((__float_as_uint(w1) >> 30) & 2u) |
+                                      ((__float_as_uint(w2) >> 29) & 4u) | ((__float_as_uint(w3) >> 28) & 8u);
+                const uint32_t hit = ~miss & valid;
+                const float g0 = (hit & 1u) ? w0 : 0.f, g1 = (hit & 2u) ? w1 : 0.f;
+                const float g2 = (hit & 4u) ? w2 : 0.f, g3 = (hit & 8u) ? w3 : 0.f;
+                float q0, q1, q2, q3;
+                upk(mul2(pk(g0, g1), pk(g0, g1)), q0, q1);
+                upk(mul2(pk(g2, g3), pk(g2, g3)), q2, q3);
+                acc = fmaf(q0, g0, acc);
+                acc = fmaf(q1, g1, acc);
+                acc = fmaf(q2, g2, acc);
+                acc = fmaf(q3, g3, acc);
+                nh += (uint32_t)__popc(hit);
+                if (FEAT == FEAT_FULL) {
+                    // r . u of the four candidates (packed), added as (cull - d2)^2 (r . u) in order
+                    const ulonglong2 ux = *reinterpret_cast<const ulonglong2*>(VX + k);
+                    const ulonglong2 uy = *reinterpret_cast<const ulonglong2*>(VY + k);
+                    const ulonglong2 uz = *reinterpret_cast<const ulonglong2*>(VZ + k);
+                    const f2 ru01 = fma2(dz01, sub2(pvz, uz.x), fma2(dy01, sub2(pvy, uy.x), mul2(dx01, sub2(pvx, ux.x))));
+                    const f2 ru23 = fma2(dz23, sub2(pvz, uz.y), fma2(dy23, sub2(pvy, uy.y), mul2(dx23, sub2(pvx, ux.y))));
+                    float r0, r1, r2, r3;
+                    upk(ru01, r0, r1);
+                    upk(ru23, r2, r3);
+                    rr = fmaf(q0, r0, rr);
+                    rr = fmaf(q1, r1, rr);
+                    rr = fmaf(q2, r2, rr);
+                    rr = fmaf(q3, r3, rr);
                 }
-                buf |= (unsigned long long)bits << nbits;
-                nbits += cnt;
+                buf |= (unsigned long long)(hit >> s0) << nbits;
+                nbits += e0 - s0;
                 if (nbits >= 32u) {
                     if (keep) my_hits[wout] = (uint32_t)buf;
                     ++wout;
@@ -754,17 +795,32 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 3 : 4) density_lane_kernel
             }
         }
         if (keep && nbits) my_hits[wout] = (uint32_t)buf;
-        if (FEAT) write_rates(sc, acc, rr, ti, rate_out);
-        write_density(sc, acc, nh, pi, ti, rho_out, p_out, ncount);
+        if (FEAT == FEAT_FULL) write_rates(sc, acc, rr, ti, rate_out);
+        const float rho_t = write_density(sc, acc, nh, pi, ti, rho_out, p_out, ncount);
+        if (FEAT && judge_part) {
+            // the ratio in FP32 (relative rounding 1e-7 against a tolerance of order 1e-2)
+            const float q = rho_t != 0.f ? fabsf(__fdividef(pi.w, rho_t) - 1.f) : 0.f;
+            judge = isfinite(q) ? q : 1.f;
+        }
+        } while (false);
+        if (FEAT && judge_part) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) judge += __shfl_xor_sync(FULL, judge, off);
+            if (lane == 0) judge_part[m] = judge;
+        }
     }
     if (lane == 0 && m == M + gridDim.x * (uint32_t)WARPS - 1u) atomicExch(counter, 0u);
 }
 
 // ---- force + integration ------------------------------------------------------------------------
 
-// Accumulators of the force pass per target: NF_PLAIN for the step; with FEAT also the time
-// derivatives of the pair terms.
-constexpr int NF_PLAIN = 6, NF_FEAT = 12;
+// Accumulators of the force pass per target: NF_PLAIN for the step; FEAT_RATE adds the density
+// rate sum, FEAT_FULL the time derivatives of the pair terms.
+constexpr int NF_PLAIN = 6, NF_RATE = 7, NF_FEAT = 12;
+template <int FEAT>
+constexpr int force_accumulators() {
+    return FEAT == FEAT_FULL ? NF_FEAT : (FEAT == FEAT_RATE ? NF_RATE : NF_PLAIN);
+}
 
 // One neighbour's pressure and viscosity terms. f[0..2] collects pres*(h-d)^2*r/d and f[3..5]
 // collects (v_j - v_i)*(h-d)/rho_j; the constant factors are applied once per particle.
@@ -775,11 +831,12 @@ constexpr int NF_PLAIN = 6, NF_FEAT = 12;
 //   dpres/dt = (p_i' + p_j') / (2 rho_j) - pres rho_j' / rho_j,
 // and f[9..11] that of the viscosity term without its neighbour-acceleration part,
 //   (v_j - v_i)(-d')/rho_j - (v_j - v_i)(h-d) rho_j' / rho_j^2.
-template <bool FEAT = false>
+// FEAT_RATE (the stale mode's judge steps): f[6] collects the Poly6 density rate sum
+// (cull - d2)^2 (r . u) (times -6 m c6 per particle).
+template <int FEAT = FEAT_NONE>
 __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, const float4& pj, const float4& vj,
                                            float h, float cull, float* f, float pdot_i = 0.f,
                                            float2 rj = make_float2(0.f, 0.f)) {
-    (void)cull;
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float d2 = dist2(rx, ry, rz);
     const float rsq = d2 > 0.f ? rsqrtf(d2) : 0.f;  // coincident pair (or self): r = 0, no push
@@ -797,7 +854,12 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
     f[3] = fmaf(vj.x - vi.x, wv, f[3]);
     f[4] = fmaf(vj.y - vi.y, wv, f[4]);
     f[5] = fmaf(vj.z - vi.z, wv, f[5]);
-    if (FEAT) {
+    if (FEAT == FEAT_RATE) {
+        const float ru = fmaf(rz, vi.z - vj.z, fmaf(ry, vi.y - vj.y, rx * (vi.x - vj.x)));
+        const float w = fmaxf(cull - d2, 0.f);
+        f[6] = fmaf(w * w, ru, f[6]);
+    }
+    if (FEAT == FEAT_FULL) {
         const float ux = vi.x - vj.x, uy = vi.y - vj.y, uz = vi.z - vj.z;
         const float ru = fmaf(rz, uz, fmaf(ry, uy, rx * ux));
         const float dp = ru * rsq;  // d'
@@ -820,8 +882,8 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
 
 // A lane's list (entries list[e * 32 + lane], e < cnt), four entries per round so their loads
 // overlap; an empty place takes the particle itself (slot self), whose terms are exactly zero.
-// FEAT: also the neighbours' rates (rate[k]) and the target's pressure rate pdot_i.
-template <bool FEAT>
+// FEAT_FULL: also the neighbours' rates (rate[k]) and the target's pressure rate pdot_i.
+template <int FEAT>
 __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t cnt, uint32_t lane, uint32_t self,
                                                 const float4& pi, const float4& vi, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vel, float h, float cull, float* f,
@@ -836,7 +898,7 @@ __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t c
         for (int u = 0; u < 4; ++u) {
             pj[u] = __ldg(pos + k[u]);
             vj[u] = __ldg(vel + k[u]);
-            rj[u] = FEAT ? __ldg(rate + k[u]) : make_float2(0.f, 0.f);
+            rj[u] = FEAT == FEAT_FULL ? __ldg(rate + k[u]) : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], h, cull, f, pdot_i, rj[u]);
@@ -845,7 +907,7 @@ __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t c
 
 // Gravity, reference-only external terms, symplectic Euler, speed clamp and wall collision
 // (update.comp:145,191-231), then the store into the state buffer.
-template <bool FEAT>
+template <int FEAT>
 __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const StepInputs& in, const float4& pi,
                                                 const float4& vi, const float* f, uint32_t ti,
                                                 float4* __restrict__ pos_a, float4* __restrict__ vel_a,
@@ -894,7 +956,8 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     vel_a[ti] = make_float4(v[0], v[1], v[2], pressure);
     if (ids_a) ids_a[ti] = ids_b[ti];
     if (accel) accel[ti] = make_float4(acc[0], acc[1], acc[2], 0.f);
-    if (FEAT) {
+    if (FEAT == FEAT_RATE) fb.out[ti] = make_float4(0.f, 0.f, 0.f, -6.f * sc.m * sc.c6 * f[6]);
+    if (FEAT == FEAT_FULL) {
         // J = d a / dt: the pair terms' derivatives over rho_i, and the internal force's share of
         // d(1/rho_i)/dt = -rho_i' / rho_i^2 (the external terms' derivatives are left out)
         float jk[3];
@@ -927,7 +990,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
                                                                uint32_t* __restrict__ err,
                                                                FeatureBuffers fb = {}) {
     (void)fb;
-    constexpr bool FEAT = false;
+    constexpr int FEAT = FEAT_NONE;
     constexpr int NF = NF_PLAIN;
     // Per warp: the slot table (candidate number -> sorted slot), then the dense path's per-lane
     // lists and its x/y/z stage; the replay path's neighbour lists use both of those regions.
@@ -1212,8 +1275,8 @@ __device__ __forceinline__ uint32_t slot_of(uint32_t q, const uint32_t P[9], con
     return q + d;
 }
 
-template <bool BATCHED, bool FEAT = false>
-__global__ void __launch_bounds__(SPH_THREADS, FEAT ? 2 : 3) force_lane_kernel(
+template <bool BATCHED, int FEAT = FEAT_NONE>
+__global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 2 : 3) force_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const StepInputs in, const uint32_t n, const uint32_t num_cells,
     const float4* __restrict__ pos_b, const float4* __restrict__ vel_b, const uint32_t* __restrict__ ids_b,
     float4* __restrict__ pos_a, float4* __restrict__ vel_a, uint32_t* __restrict__ ids_a,
@@ -1221,7 +1284,7 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 2 : 3) force_lane_kernel(
     uint32_t* __restrict__ num_nonempty,  // [2]: this pass's chunk counter
     const uint32_t* __restrict__ hits, float4* __restrict__ accel, uint32_t* __restrict__ err,
     FeatureBuffers fb = {}) {  // FEAT: the judge step's rates and feature output
-    constexpr int NF = FEAT ? NF_FEAT : NF_PLAIN;
+    constexpr int NF = force_accumulators<FEAT>();
     __shared__ uint32_t s_list[WARPS][LANE_LIST * 32];
     __shared__ uint32_t s_poff[BATCHED ? MAX_SCENES + 1 : 1];
     __shared__ uint32_t s_coff[BATCHED ? MAX_SCENES + 1 : 1];
@@ -1257,7 +1320,7 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT ? 2 : 3) force_lane_kernel(
         const uint32_t* tab = start + coff;
         const float4 pi = pos_b[tself];
         const float4 vi = vel_b[tself];
-        const float2 ri = FEAT ? fb.rate[tself] : make_float2(0.f, 0.f);
+        const float2 ri = FEAT == FEAT_FULL ? fb.rate[tself] : make_float2(0.f, 0.f);
         int32_t cx, cy, cz;
         const uint32_t c = bin_key(pi.x, pi.y, pi.z, sc.bin, sc.R, &cx, &cy, &cz);
         const uint32_t cend = min(__ldg(tab + c + 1), n);
@@ -1340,8 +1403,8 @@ constexpr int arity(void (*)(A...)) {
 // A captured step's force node is re-parameterised from ForceKernelArgs: one pointer per
 // kernel parameter.
 static_assert(arity(&force_kernel<false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
-static_assert(arity(&force_lane_kernel<false, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
-static_assert(arity(&force_lane_kernel<true, false>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
+static_assert(arity(&force_lane_kernel<false, FEAT_NONE>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
+static_assert(arity(&force_lane_kernel<true, FEAT_NONE>) == ForceKernelArgs::COUNT, "ForceKernelArgs out of date");
 
 }  // namespace
 
@@ -1390,7 +1453,8 @@ void launch_density(const DevBuffers& d, const SceneConsts& sc, const LaunchDims
     if (ld.pass_variant == PASSES_LANE)
         density_lane_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
             sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
-            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, nc, d.hits, d.err);
+            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, nc, d.hits, d.err, d.xyz,
+            d.xyz_stride);
     else
         density_kernel<false><<<ld.grid_density, SPH_THREADS, 0, s>>>(
             sc, BatchTables{}, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
@@ -1401,7 +1465,8 @@ void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const La
     if (ld.pass_variant == PASSES_LANE)
         density_lane_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
             SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
-            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err);
+            reinterpret_cast<float*>(d.vel_b) + 3, d.start, d.cell_list, d.num_nonempty, d.ncount, d.hits, d.err,
+            d.xyz, d.xyz_stride);
     else
         density_kernel<true><<<ld.grid_density, SPH_THREADS, 0, s>>>(
             SceneConsts{}, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3,
@@ -1410,16 +1475,16 @@ void launch_density_batched(const DevBuffers& d, const BatchTables& bt, const La
 
 // The force pass of variant `ld.pass_variant` on a persistent grid sized from that kernel's
 // occupancy; FEAT (the judge steps): the lane kernel with its feature buffers, on a grid of its
-// own occupancy (more registers per thread than the plain kernel).
-template <bool BATCHED, bool FEAT>
+// own occupancy.
+template <bool BATCHED, int FEAT>
 void launch_force_any(const DevBuffers& d, const SceneConsts& sc, const BatchTables& bt, const StepInputs& in,
                       const LaunchDims& ld, FeatureBuffers fb, cudaStream_t s) {
-    const bool lane = FEAT || ld.pass_variant == PASSES_LANE;
+    const bool lane = FEAT != FEAT_NONE || ld.pass_variant == PASSES_LANE;
     int grid = ld.grid_force;
-    if (FEAT) {
+    if (FEAT != FEAT_NONE) {
         static int blocks = 0;
         if (!blocks) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, force_lane_kernel<BATCHED, true>, SPH_THREADS, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, force_lane_kernel<BATCHED, FEAT>, SPH_THREADS, 0);
             if (blocks <= 0) blocks = 1;
         }
         grid = ld.sms * blocks;
@@ -1436,48 +1501,61 @@ void launch_force_any(const DevBuffers& d, const SceneConsts& sc, const BatchTab
 
 void launch_force(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
                   cudaStream_t s) {
-    launch_force_any<false, false>(d, sc, BatchTables{}, in, ld, FeatureBuffers{}, s);
+    launch_force_any<false, FEAT_NONE>(d, sc, BatchTables{}, in, ld, FeatureBuffers{}, s);
 }
 
 void launch_force_batched(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
                           cudaStream_t s) {
-    launch_force_any<true, false>(d, SceneConsts{}, bt, in, ld, FeatureBuffers{}, s);
+    launch_force_any<true, FEAT_NONE>(d, SceneConsts{}, bt, in, ld, FeatureBuffers{}, s);
 }
 
 void launch_force_feat(const DevBuffers& d, const SceneConsts& sc, const StepInputs& in, const LaunchDims& ld,
-                       FeatureBuffers fb, cudaStream_t s) {
-    launch_force_any<false, true>(d, sc, BatchTables{}, in, ld, fb, s);
+                       int level, FeatureBuffers fb, cudaStream_t s) {
+    if (level == FEAT_FULL)
+        launch_force_any<false, FEAT_FULL>(d, sc, BatchTables{}, in, ld, fb, s);
+    else
+        launch_force_any<false, FEAT_RATE>(d, sc, BatchTables{}, in, ld, fb, s);
 }
 
 void launch_force_batched_feat(const DevBuffers& d, const BatchTables& bt, const StepInputs& in, const LaunchDims& ld,
-                               FeatureBuffers fb, cudaStream_t s) {
-    launch_force_any<true, true>(d, SceneConsts{}, bt, in, ld, fb, s);
+                               int level, FeatureBuffers fb, cudaStream_t s) {
+    if (level == FEAT_FULL)
+        launch_force_any<true, FEAT_FULL>(d, SceneConsts{}, bt, in, ld, fb, s);
+    else
+        launch_force_any<true, FEAT_RATE>(d, SceneConsts{}, bt, in, ld, fb, s);
 }
 
-// The judge steps' density pass: the lane kernel with its rate output, on a grid of its own
-// occupancy, whatever ld.pass_variant says (its bit strings are the lane force pass's).
-template <bool BATCHED>
+// The judge steps' density pass: the lane kernel with its judge sums (and, FEAT_FULL, rate)
+// output, on a grid of its own occupancy, whatever ld.pass_variant says (its bit strings are the
+// lane force pass's).
+template <bool BATCHED, int FEAT>
 void launch_density_any_feat(const DevBuffers& d, const SceneConsts& sc, const BatchTables& bt, const LaunchDims& ld,
-                             float2* rate, cudaStream_t s) {
+                             const float* vxyz, float2* rate, float* judge_part, cudaStream_t s) {
     static int blocks = 0;
     if (!blocks) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, density_lane_kernel<BATCHED, true>, SPH_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, density_lane_kernel<BATCHED, FEAT>, SPH_THREADS, 0);
         if (blocks <= 0) blocks = 1;
     }
     uint32_t* nc = BATCHED ? d.ncount : ((sc.flags & WC_FLAG_NEIGHBOR_COUNTS) ? d.ncount : nullptr);
-    density_lane_kernel<BATCHED, true><<<ld.sms * blocks, SPH_THREADS, 0, s>>>(
+    density_lane_kernel<BATCHED, FEAT><<<ld.sms * blocks, SPH_THREADS, 0, s>>>(
         sc, bt, d.n, d.num_cells, d.pos_b, reinterpret_cast<float*>(d.pos_b) + 3, reinterpret_cast<float*>(d.vel_b) + 3,
-        d.start, d.cell_list, d.num_nonempty, nc, d.hits, d.err, d.vel_b, rate);
+        d.start, d.cell_list, d.num_nonempty, nc, d.hits, d.err, d.xyz, d.xyz_stride, d.vel_b, vxyz, rate, judge_part);
 }
 
-void launch_density_feat(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, float2* rate,
-                         cudaStream_t s) {
-    launch_density_any_feat<false>(d, sc, BatchTables{}, ld, rate, s);
+void launch_density_feat(const DevBuffers& d, const SceneConsts& sc, const LaunchDims& ld, int level,
+                         const float* vxyz, float2* rate, float* judge_part, cudaStream_t s) {
+    if (level == FEAT_FULL)
+        launch_density_any_feat<false, FEAT_FULL>(d, sc, BatchTables{}, ld, vxyz, rate, judge_part, s);
+    else
+        launch_density_any_feat<false, FEAT_RATE>(d, sc, BatchTables{}, ld, vxyz, rate, judge_part, s);
 }
 
-void launch_density_batched_feat(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, float2* rate,
-                                 cudaStream_t s) {
-    launch_density_any_feat<true>(d, SceneConsts{}, bt, ld, rate, s);
+void launch_density_batched_feat(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, int level,
+                                 const float* vxyz, float2* rate, float* judge_part, cudaStream_t s) {
+    if (level == FEAT_FULL)
+        launch_density_any_feat<true, FEAT_FULL>(d, SceneConsts{}, bt, ld, vxyz, rate, judge_part, s);
+    else
+        launch_density_any_feat<true, FEAT_RATE>(d, SceneConsts{}, bt, ld, vxyz, rate, judge_part, s);
 }
 
 const void* force_kernel_symbol(int pass_variant) {
