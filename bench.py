@@ -721,6 +721,7 @@ def run_batch(args):
         "tuning": {"density_blocks_per_sm": tuning.density_blocks_per_sm,
                    "force_blocks_per_sm": tuning.force_blocks_per_sm,
                    "stream_blocks_per_sm": tuning.stream_blocks_per_sm, "cell_factor": tuning.cell_factor,
+                   "pass_variant": "lane per target" if tuning.pass_variant == _abi.WC_PASSES_LANE else "team per cell",
                    "trials": tuning.trials, "tune_seconds": tune_s},
         "e2e": {"value": n * e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps,

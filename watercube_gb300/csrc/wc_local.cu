@@ -56,6 +56,7 @@ constexpr uint32_t TILE = 128;
 constexpr uint32_t MLP_THREADS = 128;
 constexpr uint32_t MLP_CTAS_PER_SM = 6;
 constexpr uint32_t TMEM_COLS = 64;
+static_assert(MLP_THREADS == TILE && TILE == 128 && OUT == 16, "mlp_kernel: one thread per row, 4 warps, 16 outputs");
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
 // The network's time unit: its J and density-rate inputs are J DT_REF / a_s and
 // 100 rhodot DT_REF / rho, and it learns the residual of the Taylor term in units of
@@ -523,16 +524,24 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
                 }
             }
             if (SUMS) {
+                // the outputs as floats into the hidden tile (layer 3's MMAs have read it), rows
+                // 17 floats apart so that a column's 16-row runs hit distinct banks
+                float* sy = reinterpret_cast<float*>(sm.h);
 #pragma unroll
-                for (uint32_t j = 0; j < OUT; ++j) {
-                    float v = y[j];
-#pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-                    if (lane == 0) sm_sums[warp][j] = v;
-                }
+                for (uint32_t j = 0; j < OUT; ++j) sy[tid * 17u + j] = y[j];
             }
         }
         if (SUMS) {
+            __syncthreads();
+            // thread 16 g + j adds column j over rows 16 g .. 16 g + 15; the two row groups of a
+            // warp meet in one shuffle, the four warps in a fixed order
+            const float* sy = reinterpret_cast<const float*>(sm.h);
+            const uint32_t g = tid >> 4, jc = tid & 15u;
+            float v = 0.f;
+#pragma unroll
+            for (uint32_t r = 0; r < 16; ++r) v += sy[(16u * g + r) * 17u + jc];
+            v += __shfl_xor_sync(0xffffffffu, v, 16);
+            if ((lane & 16u) == 0) sm_sums[warp][jc] = v;
             __syncthreads();
             if (tid < OUT) cta_sum += ((sm_sums[0][tid] + sm_sums[1][tid]) + sm_sums[2][tid]) + sm_sums[3][tid];
         }

@@ -399,13 +399,14 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(const GemmArgs g, uint32_
 // slot holds an A and a B slice (4 slots, 2 in flight). Warp 4 (lane 0) waits for `full`, issues
 // the slice's four MMAs into one of two 128-column accumulators in tensor memory and commits them
 // to the slot's `empty` barrier (the slot may be refilled) and, after a tile's last slice, to the
-// accumulator's `acc_full` barrier. Warps 5..8 wait for `acc_full`, read their 32 accumulator
-// rows each (warp w reads lanes 32 (w % 4) ..), apply the epilogue and arrive on `acc_empty`. So
+// accumulator's `acc_full` barrier. Warps 5..12 wait for `acc_full`, read 32 accumulator rows x 64
+// columns each (warp w reads lanes 32 (w % 4) ..), apply the epilogue and arrive on `acc_empty`. So
 // the copies of the next slices, the MMAs of one tile and the epilogue of the previous tile
 // overlap. Every wait is bounded; a wait that runs out stops the CTA's loops
 // (DEVERR_MMA_TIMEOUT) and the CTA still frees its tensor memory.
-constexpr int PIPE_PRODUCERS = 4;  // warps 0..3 copy, warp 4 issues the MMAs, warps 5..8 drain
-constexpr int PIPE_THREADS = 32 * (PIPE_PRODUCERS + 1 + 4);
+constexpr int PIPE_PRODUCERS = 4;  // warps 0..3 copy, warp 4 issues the MMAs, warps 5..12 drain
+constexpr int PIPE_EPILOGUE = 8;   // two warps per 32-lane quarter of the accumulator, 64 columns each
+constexpr int PIPE_THREADS = 32 * (PIPE_PRODUCERS + 1 + PIPE_EPILOGUE);
 constexpr uint32_t PIPE_TMEM_COLS = 256;
 constexpr uint32_t TILE_BYTES = BM * BK * 2;  // one 128 x 64 BF16 operand slice, 16 KB
 // Resident B (RB): the whole B^T tile [128 x k] stays in shared memory, loaded once per CTA,
@@ -475,7 +476,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
         }
         for (int q = 0; q < 2; ++q) {
             mbar_init(&acc_full[q], 1);
-            mbar_init(&acc_empty[q], 4);  // one arrival per epilogue warp
+            mbar_init(&acc_empty[q], PIPE_EPILOGUE);  // one arrival per epilogue warp
         }
         mbar_init(&b_full, 32 * PIPE_PRODUCERS);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -580,8 +581,10 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
         }
         __syncwarp();
     } else {
-        // epilogue: warp w reads accumulator lanes 32 (w % 4) .. + 31
+        // epilogue: warp w reads accumulator lanes 32 (w % 4) .. + 31 (the lanes its position in
+        // the warpgroup may address), columns 64 half .. + 63
         const uint32_t quarter = warp & 3u;
+        const uint32_t half = (warp - (uint32_t)(PIPE_PRODUCERS + 1)) / 4u;
         uint32_t t = 0;
         for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
             const uint32_t b = t & 1u;
@@ -595,7 +598,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
             const uint32_t m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
             const uint32_t row = m0 + 32u * quarter + lane;
             const bool row_ok = row < g.m;
-            for (uint32_t c0 = 0; c0 < BN; c0 += 32) {
+            for (uint32_t c0 = 64u * half; c0 < 64u * half + 64u; c0 += 32) {
                 uint32_t v[32];
                 const uint32_t taddr = tmem + ((32u * quarter) << 16) + b * (uint32_t)BN + c0;
                 asm volatile(

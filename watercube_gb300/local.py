@@ -153,3 +153,39 @@ def load_weights(path: Path = DEFAULT_WEIGHTS, **overrides) -> LocalNet:
                    **overrides)
     net.set_params(z["params"])
     return net
+
+
+def main(argv=None) -> int:
+    """python -m watercube_gb300.local: a fast rollout of the dam break (the benchmark's scene) in
+    one mode, with its statistics printed as JSON."""
+    import argparse
+    import json
+
+    from .fluid import dam_break_params, finalize, generate_dam_break
+
+    ap = argparse.ArgumentParser(description=main.__doc__.split("\n")[0])
+    ap.add_argument("--particles", type=int, default=1048576)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--ages", type=int, default=3, help="skipped steps per cycle (K - 1)")
+    ap.add_argument("--mode", choices=["stale", "taylor", "network"], default="network")
+    ap.add_argument("--tolerance", type=float, default=0.01)
+    ap.add_argument("--weights", type=Path, default=None, help="default: weights/local_k{ages + 1}.npz")
+    a = ap.parse_args(argv)
+    check(lib().wc_set_device(0), "select device")
+    p = finalize(dam_break_params(a.particles))
+    dt = 2.5e-4 * (1048576.0 / a.particles) ** (1.0 / 3.0)
+    mode = {"stale": WC_LOCAL_STALE, "taylor": WC_LOCAL_TAYLOR, "network": WC_LOCAL_NETWORK}[a.mode]
+    net = None
+    if mode == WC_LOCAL_NETWORK:
+        net = load_weights(a.weights or DEFAULT_WEIGHTS.with_name(f"local_k{a.ages + 1}.npz"))
+    with Fluid.create("rollout", p) as f:
+        f.setup(generate_dam_break(p, 0))
+        stats = rollout(f, dt, a.steps, ages=a.ages, tolerance=a.tolerance, net=net, mode=mode)
+    if net is not None:
+        net.close()
+    print(json.dumps({"mode": a.mode, "particles": a.particles, "dt": dt, "K": a.ages + 1, **stats}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
