@@ -1276,7 +1276,7 @@ __device__ __forceinline__ uint32_t slot_of(uint32_t q, const uint32_t P[9], con
 }
 
 template <bool BATCHED, int FEAT = FEAT_NONE>
-__global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 2 : 4) force_lane_kernel(
+__global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 2 : 3) force_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const StepInputs in, const uint32_t n, const uint32_t num_cells,
     const float4* __restrict__ pos_b, const float4* __restrict__ vel_b, const uint32_t* __restrict__ ids_b,
     float4* __restrict__ pos_a, float4* __restrict__ vel_a, uint32_t* __restrict__ ids_a,
