@@ -4,11 +4,10 @@ tests/ to check the CUDA path, never by the solver.
   pair_sums    the judge step's pass sums per particle: the SPH acceleration (the update
                shader's pressure, viscosity and gravity terms, assets/fluid/update.comp:149-195),
                the Poly6 density rate -6 m c6 sum (cull - d2)^2 (r . (v_i - v_j)), and
-               J = d a / dt when the positions move with their velocities and the densities and
-               pressures follow them (the density pass's rates; velocities held, so the viscosity
-               term's neighbour-acceleration part is not in J). Neighbours are the pairs the
-               solver's test selects (float32 d2 <= cull, the reference's |r| < h), evaluated in
-               float64.
+               J = d a / dt of the pressure term when the positions move with their velocities
+               and the densities and pressures follow them (the density pass's rates); the
+               viscosity term's derivative is not in J. Neighbours are the pairs the solver's test
+               selects (float32 d2 <= cull, the reference's |r| < h), evaluated in float64.
   inputs       the network's 19 inputs (unrounded).
   forward      the network with the BF16 roundings of the tensor-core path (inputs, weights and
                hidden activations rounded to BF16, sums in float64).
@@ -95,16 +94,14 @@ def pair_sums(p, sorted_state: np.ndarray, cull: float):
     fp = np.zeros((n, 3))
     fv = np.zeros((n, 3))
     jp = np.zeros((n, 3))
-    jv = np.zeros((n, 3))
     np.add.at(fp, i, coef[:, None] * r)
     np.add.at(fv, i, (v[j] - v[i]) * (hd / rho[j])[:, None])
     np.add.at(jp, i, (dcoef * dp + dpres * hd * hd * inv_d)[:, None] * r + coef[:, None] * u)
-    np.add.at(jv, i, u * (dp / rho[j] + hd * rate[j] / (rho[j] * rho[j]))[:, None])
     g = np.array(list(p.gravity), np.float64)
     inv = 1.0 / (rho + 1e-16)
-    internal = (fp_scale * fp + fv_scale * fv) * inv[:, None]
-    acc = internal + g[None, :] * (rho * inv)[:, None]
-    jerk = (fp_scale * jp + fv_scale * jv) * inv[:, None] - (rate * inv)[:, None] * internal
+    pressure_acc = fp_scale * fp * inv[:, None]
+    acc = pressure_acc + fv_scale * fv * inv[:, None] + g[None, :] * (rho * inv)[:, None]
+    jerk = fp_scale * jp * inv[:, None] - (rate * inv)[:, None] * pressure_acc
     return acc, jerk, rate
 
 

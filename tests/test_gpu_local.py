@@ -150,3 +150,15 @@ def test_network_mode_needs_a_network(gpu):
     with fluid(p, st) as f:
         with pytest.raises(_abi.WatercubeError):
             rollout(f, 1e-3, 8, ages=3, mode=WC_LOCAL_NETWORK)
+
+
+def test_rollout_command_runs_each_mode(gpu, capsys):
+    """python -m watercube_gb300.local: a short rollout of a small dam break in every mode."""
+    import json
+
+    from watercube_gb300.local import main
+
+    for mode in ("stale", "taylor", "network"):
+        assert main(["--particles", "16384", "--steps", "8", "--mode", mode]) == 0
+        r = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+        assert r["mode"] == mode and r["steps"] == 8 and r["judged"] >= 1 and r["mean_density_error"] < 0.01

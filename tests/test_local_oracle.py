@@ -36,10 +36,11 @@ def test_backward_matches_central_differences():
 
 
 def test_pair_sums_are_the_time_derivatives():
-    """J and the density rate are d/dt of the SPH acceleration and of the Poly6 density when the
-    positions move with their velocities (velocities held) and the density pass recomputes the
+    """J and the density rate are d/dt of the SPH acceleration's pressure term and of the Poly6
+    density when the positions move with their velocities and the density pass recomputes the
     densities and pressures of the moved state: finite differences of the FP64 oracle's density
-    pass and of the pair sums, for both equations of state."""
+    pass and of the pair sums without viscosity (J leaves the viscosity term's derivative out),
+    for both equations of state."""
     scipy = pytest.importorskip("scipy")
     del scipy
     from oracle.oracle import Oracle, to64
@@ -48,6 +49,7 @@ def test_pair_sums_are_the_time_derivatives():
     for eos in (1, 0):  # WC_EOS_LINEAR, WC_EOS_DESBRUN_CUBIC
         p = o.dam_break_params(4096)
         p.eos = eos
+        p.viscosity = 0.0
         st = o.generate_dam_break(p, 0)
         st["velocity"] = np.random.default_rng(1).normal(0.0, 0.3, (4096, 3)).astype(np.float32)
         srt, _, _, counts, offsets = o.sort(p, st)

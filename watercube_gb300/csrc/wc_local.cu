@@ -486,16 +486,15 @@ __global__ void __launch_bounds__(MLP_THREADS, MLP_CTAS_PER_SM) mlp_kernel(uint3
         ok = s_failed ? false : mbar_wait(mb, phase);
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        {
-            // the MMAs have read h1 (their commit arrived): h2 overwrites it
-            float y[64];
-            tmem_ld32(tlane, y);
-            tmem_ld32(tlane + 32u, y + 32);
+        // the MMAs have read all of h1 (their commit arrived): h2 overwrites it, 32 columns at a
+        // time (each thread writes its own row only)
+        for (uint32_t c0 = 0; c0 < HID; c0 += 32) {
+            float y[32];
+            tmem_ld32(tlane + c0, y);
 #pragma unroll
-            for (int j = 0; j < 64; ++j) y[j] = fmaxf(y[j] + sm.b2[j], 0.f);
-            __syncwarp();
+            for (int j = 0; j < 32; ++j) y[j] = fmaxf(y[j] + sm.b2[c0 + j], 0.f);
 #pragma unroll
-            for (uint32_t g = 0; g < 8; ++g) put8(sm.h, tid, 8u * g, HID, y + 8 * g);
+            for (uint32_t g = 0; g < 4; ++g) put8(sm.h, tid, c0 + 8u * g, HID, y + 8 * g);
         }
         if (!ok) atomicOr(&s_failed, 1);
         // layer 3: [128 x 64] . W3 -> 16 columns

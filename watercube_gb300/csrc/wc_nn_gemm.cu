@@ -23,6 +23,7 @@
 // shared memory when it fits, two accumulators, see below) for row-major operands without a
 // split of K — the forward layers and the input gradients; gemm_kernel (one tile per CTA, two operand buffers) for the transposed
 // weight-gradient operands and split-K.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -450,6 +451,52 @@ __device__ __forceinline__ void pipe_stage_copy(const OperandSrc& s, __nv_bfloat
     }
 }
 
+// The epilogue warps of the persistent kernels: for each of the CTA's tiles wait for its
+// accumulator (acc_full[t & 1]), read 32 rows (lanes 32 quarter ..) x 64 columns (64 half ..)
+// with tcgen05.ld, apply the epilogue, and hand the accumulator back (acc_empty). A wait that runs
+// out sets `failed`.
+__device__ __forceinline__ void drain_accumulators(const GemmArgs& g, uint32_t tmem, uint64_t* acc_full,
+                                                   uint64_t* acc_empty, volatile int* failed, uint32_t ntiles,
+                                                   uint32_t tiles_n, uint32_t nslices, uint32_t quarter,
+                                                   uint32_t half, uint32_t lane) {
+    uint32_t t = 0;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
+        const uint32_t b = t & 1u;
+        bool ok = !*failed && mbar_wait(smem_addr(&acc_full[b]), (t >> 1) & 1u);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) {
+            if (lane == 0) *failed = 1;
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        const uint32_t row = m0 + 32u * quarter + lane;
+        const bool row_ok = row < g.m;
+        for (uint32_t c0 = 64u * half; c0 < 64u * half + 64u; c0 += 32) {
+            uint32_t v[32];
+            const uint32_t taddr = tmem + ((32u * quarter) << 16) + b * (uint32_t)BN + c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (!row_ok || n0 + c0 >= g.n) continue;
+            float x[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) x[j] = nslices ? __uint_as_float(v[j]) : 0.f;
+            epilogue_store(g, x, row, n0 + c0, min(32u, g.n - (n0 + c0)), 0u);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[b]);
+    }
+}
+
 template <bool RB>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmArgs g, uint32_t* err) {
     constexpr int STAGES = PipeShape<RB>::STAGES, LAG = PipeShape<RB>::LAG;
@@ -585,46 +632,166 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmAr
         // the warpgroup may address), columns 64 half .. + 63
         const uint32_t quarter = warp & 3u;
         const uint32_t half = (warp - (uint32_t)(PIPE_PRODUCERS + 1)) / 4u;
-        uint32_t t = 0;
-        for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
-            const uint32_t b = t & 1u;
-            bool ok = !*failed && mbar_wait(smem_addr(&acc_full[b]), (t >> 1) & 1u);
-            ok = __all_sync(0xffffffffu, ok);
-            if (!ok) {
-                if (lane == 0) *failed = 1;
-                break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
-            const uint32_t row = m0 + 32u * quarter + lane;
-            const bool row_ok = row < g.m;
-            for (uint32_t c0 = 64u * half; c0 < 64u * half + 64u; c0 += 32) {
-                uint32_t v[32];
-                const uint32_t taddr = tmem + ((32u * quarter) << 16) + b * (uint32_t)BN + c0;
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                    : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (!row_ok || n0 + c0 >= g.n) continue;
-                float x[32];
-#pragma unroll
-                for (int j = 0; j < 32; ++j) x[j] = nslices ? __uint_as_float(v[j]) : 0.f;
-                epilogue_store(g, x, row, n0 + c0, min(32u, g.n - (n0 + c0)), 0u);
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_empty[b]);
-        }
+        drain_accumulators(g, tmem, acc_full, acc_empty, failed, ntiles, tiles_n, nslices, quarter, half, lane);
     }
     __syncthreads();
     if (*failed && threadIdx.x == 0 && err) atomicOr(err, DEVERR_MMA_TIMEOUT);
     if (warp == PIPE_PRODUCERS) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(PIPE_TMEM_COLS));
+    }
+}
+
+// ---- TMA variant: plain row-major A and B^T, B resident ----------------------------------------
+//
+// For A without a row gather or a second source, and B^T of one column of tiles (n <= 128,
+// k <= 64 RB_MAX_SLICES): one thread of warp 0 copies the operands with cp.async.bulk.tensor
+// (TMA) in the 128-byte-swizzled K-major layout — B^T once per CTA (barrier `b_full`), then the
+// A slices of the CTA's tiles into a 6-slot ring, each copy completing its slot's `full` barrier
+// by its byte count (mbarrier expect_tx); warp 1 issues the MMAs with 128-byte-swizzle
+// descriptors (a K step of 16 is a 32-byte advance inside the swizzle atom); warps 2..9 drain
+// the accumulators as in gemm_pipe_kernel. The tensor maps cover this GPU's own global memory;
+// no multicast.
+constexpr int TMA_STAGES = 6;
+constexpr int TMA_THREADS = 32 * (2 + PIPE_EPILOGUE);
+
+// Shared-memory descriptor of a K-major operand tile in the 128-byte swizzle layout: rows of
+// 128 bytes, 8-row groups 1,024 bytes apart (SBO), the leading-byte offset unused, version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// One 64 x 128 box (64 K elements, 128 rows) of a 2-D BF16 tensor map into shared memory; the
+// copy completes `bar` by its bytes. x (the K coordinate) is a multiple of 64 elements (128 B).
+__device__ __forceinline__ void tma_load_box(const CUtensorMap* map, void* dst, uint32_t x, uint32_t y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__global__ void __launch_bounds__(TMA_THREADS, 1) gemm_tma_kernel(const GemmArgs g,
+                                                                  const __grid_constant__ CUtensorMap map_a,
+                                                                  const __grid_constant__ CUtensorMap map_b,
+                                                                  uint32_t* err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t full[TMA_STAGES], empty[TMA_STAGES], acc_full[2], acc_empty[2], b_full;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_failed;
+    volatile int* failed = &s_failed;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t tiles_m = (g.m + BM - 1) / BM, tiles_n = 1u;
+    const uint32_t ntiles = tiles_m;
+    const uint32_t nslices = (g.k + BK - 1) / BK;
+    // [B^T slices 0 .. nslices)[A ring], every slot 16 KB and 1,024-byte aligned
+    unsigned char* const ring = smem_raw + nslices * TILE_BYTES;
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < TMA_STAGES; ++q) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], 1);
+        }
+        for (int q = 0; q < 2; ++q) {
+            mbar_init(&acc_full[q], 1);
+            mbar_init(&acc_empty[q], PIPE_EPILOGUE);
+        }
+        mbar_init(&b_full, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_failed = 0;
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(PIPE_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // B^T once, then the A slices of every tile through the ring
+            mbar_expect_tx(&b_full, nslices * TILE_BYTES);
+            for (uint32_t sl = 0; sl < nslices; ++sl) tma_load_box(&map_b, smem_raw + sl * TILE_BYTES, sl * BK, 0u, &b_full);
+            uint32_t it = 0;
+            for (uint32_t tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x) {
+                const uint32_t m0 = tile * BM;
+                for (uint32_t sl = 0; sl < nslices; ++sl, ++it) {
+                    const uint32_t st = it % TMA_STAGES;
+                    if (it >= (uint32_t)TMA_STAGES &&
+                        !mbar_wait(smem_addr(&empty[st]), ((it / TMA_STAGES) - 1u) & 1u)) {
+                        *failed = 1;
+                        break;
+                    }
+                    mbar_expect_tx(&full[st], TILE_BYTES);
+                    tma_load_box(&map_a, ring + st * TILE_BYTES, sl * BK, m0, &full[st]);
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // MMA issue (one thread)
+        if (lane == 0) {
+            uint32_t it = 0, t = 0;
+            if (!mbar_wait(smem_addr(&b_full), 0u)) *failed = 1;
+            for (uint32_t tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x, ++t) {
+                const uint32_t b = t & 1u;
+                if (t >= 2 && !mbar_wait(smem_addr(&acc_empty[b]), ((t >> 1) - 1u) & 1u)) {
+                    *failed = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc_addr = tmem + b * (uint32_t)BN;
+                for (uint32_t sl = 0; sl < nslices; ++sl, ++it) {
+                    const uint32_t st = it % TMA_STAGES;
+                    if (!mbar_wait(smem_addr(&full[st]), (it / TMA_STAGES) & 1u)) {
+                        *failed = 1;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t a_base = smem_addr(ring + st * TILE_BYTES);
+                    const uint32_t b_base = smem_addr(smem_raw + sl * TILE_BYTES);
+#pragma unroll
+                    for (uint32_t j = 0; j < BK / 16; ++j) {
+                        const uint64_t ad = sw128_desc(a_base + 32u * j);
+                        const uint64_t bd = sw128_desc(b_base + 32u * j);
+                        const uint32_t acc = (sl > 0 || j > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc_addr),
+                            "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_addr(&empty[st]))
+                                 : "memory");
+                }
+                if (*failed) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_addr(&acc_full[b]))
+                             : "memory");
+            }
+        }
+        __syncwarp();
+    } else {
+        // warps 2..9: quarter w % 4, columns 64 ((w - 2) / 4) ..
+        drain_accumulators(g, tmem, acc_full, acc_empty, failed, ntiles, tiles_n, nslices, warp & 3u, (warp - 2u) / 4u,
+                           lane);
+    }
+    __syncthreads();
+    if (*failed && threadIdx.x == 0 && err) atomicOr(err, DEVERR_MMA_TIMEOUT);
+    if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(PIPE_TMEM_COLS));
     }
@@ -659,6 +826,37 @@ size_t pipe_smem_bytes(bool rb, uint32_t k) {
               : (size_t)PipeShape<false>::STAGES * 2u * TILE_BYTES;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (null when unavailable: the
+// cp.async kernel then serves every shape).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// A 2-D BF16 row-major tensor [outer x inner] with rows `stride_bytes` apart, read in boxes of
+// 64 x 128 elements with the 128-byte swizzle, out-of-range elements as zeros.
+bool encode_operand(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, uint64_t stride_bytes) {
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn || reinterpret_cast<uintptr_t>(base) % 16u || stride_bytes % 16u || inner == 0 || outer == 0) return false;
+    const cuuint64_t dims[2] = {inner, outer};
+    const cuuint64_t strides[1] = {stride_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
+    const cuuint32_t elem[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, elem,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s) {
     const wc_status st = check_gemm(g);
     if (st != WC_OK || g.m == 0 || g.n == 0) return st;
@@ -679,6 +877,22 @@ wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s) {
         const uint32_t tiles = ((g.m + BM - 1) / BM) * ((g.n + BN - 1) / BN);
         const uint32_t grid = tiles < (uint32_t)sms ? tiles : (uint32_t)sms;
         const bool rb = g.n <= (uint32_t)BN && (g.k + BK - 1) / BK <= RB_MAX_SLICES;
+        if (rb && !g.a_rows && !g.a2) {
+            // plain A: the TMA kernel, when both operands have tensor maps
+            CUtensorMap ma, mb;
+            if (encode_operand(&ma, g.a, g.k, g.m, 2ull * g.lda) && encode_operand(&mb, g.b, g.k, g.n, 2ull * g.ldb)) {
+                static bool tma_attr = false;
+                if (!tma_attr) {
+                    cudaFuncSetAttribute(gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)pipe_smem_bytes(true, RB_MAX_SLICES * BK));
+                    tma_attr = true;
+                }
+                gemm_tma_kernel<<<grid, TMA_THREADS, pipe_smem_bytes(true, g.k), s>>>(g, ma, mb, err);
+                const cudaError_t e = cudaGetLastError();
+                if (e != cudaSuccess) return fail(WC_ERR_CUDA, "gemm launch: %s", cudaGetErrorString(e));
+                return WC_OK;
+            }
+        }
         if (rb)
             gemm_pipe_kernel<true><<<grid, PIPE_THREADS, pipe_smem_bytes(true, g.k), s>>>(g, err);
         else

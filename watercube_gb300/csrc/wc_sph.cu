@@ -771,6 +771,8 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 3 : 4) densit
                 nh += (uint32_t)__popc(hit);
                 if (FEAT == FEAT_FULL) {
                     // r . u of the four candidates (packed), added as (cull - d2)^2 (r . u) in order
+                    // (loaded for every quad: skipping the quads without hits diverges and was
+                    // slower)
                     const ulonglong2 ux = *reinterpret_cast<const ulonglong2*>(VX + k);
                     const ulonglong2 uy = *reinterpret_cast<const ulonglong2*>(VY + k);
                     const ulonglong2 uz = *reinterpret_cast<const ulonglong2*>(VZ + k);
@@ -816,7 +818,7 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 3 : 4) densit
 
 // Accumulators of the force pass per target: NF_PLAIN for the step; FEAT_RATE adds the density
 // rate sum, FEAT_FULL the time derivatives of the pair terms.
-constexpr int NF_PLAIN = 6, NF_RATE = 7, NF_FEAT = 12;
+constexpr int NF_PLAIN = 6, NF_RATE = 7, NF_FEAT = 9;
 template <int FEAT>
 constexpr int force_accumulators() {
     return FEAT == FEAT_FULL ? NF_FEAT : (FEAT == FEAT_RATE ? NF_RATE : NF_PLAIN);
@@ -824,13 +826,14 @@ constexpr int force_accumulators() {
 
 // One neighbour's pressure and viscosity terms. f[0..2] collects pres*(h-d)^2*r/d and f[3..5]
 // collects (v_j - v_i)*(h-d)/rho_j; the constant factors are applied once per particle.
-// FEAT (the learned rollout's judge steps): the time derivatives of both, with u = v_i - v_j the
-// rate of r, d' = r.u/d the rate of d and the density pass's rates (rho_j', p_j' in rj, p_i' in
-// pdot_i): f[6..8] collects d/dt of the pressure term,
+// FEAT_FULL (the fast rollout's judge steps): the time derivative of the pressure term, with
+// u = v_i - v_j the rate of r, d' = r.u/d the rate of d and the density pass's rates (rho_j',
+// p_j' in rj, p_i' in pdot_i): f[6..8] collects
 //   (dpres/dt (h-d)^2/d + pres d((h-d)^2/d)/dd d') r + coef u,
-//   dpres/dt = (p_i' + p_j') / (2 rho_j) - pres rho_j' / rho_j,
-// and f[9..11] that of the viscosity term without its neighbour-acceleration part,
-//   (v_j - v_i)(-d')/rho_j - (v_j - v_i)(h-d) rho_j' / rho_j^2.
+//   dpres/dt = (p_i' + p_j') / (2 rho_j) - pres rho_j' / rho_j.
+// The viscosity term's derivative is left out: it changes the first-order extrapolation of the
+// acceleration by a few percent of its error (1.03 % -> 1.08 % at the first skipped step, FP64
+// oracle, 32,768-particle dam break after 300 steps).
 // FEAT_RATE (the stale mode's judge steps): f[6] collects the Poly6 density rate sum
 // (cull - d2)^2 (r . u) (times -6 m c6 per particle).
 template <int FEAT = FEAT_NONE>
@@ -873,10 +876,6 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
             f[7] = fmaf(cr, ry, fmaf(coef, uy, f[7]));
             f[8] = fmaf(cr, rz, fmaf(coef, uz, f[8]));
         }
-        const float wj = inv_rho * fmaf(wv, rj.x, dp);
-        f[9] = fmaf(ux, wj, f[9]);
-        f[10] = fmaf(uy, wj, f[10]);
-        f[11] = fmaf(uz, wj, f[11]);
     }
 }
 
@@ -937,7 +936,10 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     float v[3], x[3], acc[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const float force = fp_scale * f[a] + fv_scale * f[3 + a] + ext[a];
+        // explicit fused operations: the judge steps' variants reuse the products below, and the
+        // sum must round the same way in every variant (a judged rollout that reverts every cycle
+        // equals plain SPH bit for bit)
+        const float force = fmaf(fp_scale, f[a], fmaf(fv_scale, f[3 + a], ext[a]));
         acc[a] = force * inv;
         float va = vin[a] + acc[a] * in.dt;
         if (sc.flags & WC_FLAG_SPEED_CLAMP) va = fminf(fmaxf(va, -sc.max_speed), sc.max_speed);
@@ -958,13 +960,14 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
     if (accel) accel[ti] = make_float4(acc[0], acc[1], acc[2], 0.f);
     if (FEAT == FEAT_RATE) fb.out[ti] = make_float4(0.f, 0.f, 0.f, -6.f * sc.m * sc.c6 * f[6]);
     if (FEAT == FEAT_FULL) {
-        // J = d a / dt: the pair terms' derivatives over rho_i, and the internal force's share of
-        // d(1/rho_i)/dt = -rho_i' / rho_i^2 (the external terms' derivatives are left out)
+        // J = d a / dt of the pressure term: its pair derivatives over rho_i and its share of
+        // d(1/rho_i)/dt = -rho_i' / rho_i^2 (the viscosity and external terms' derivatives are
+        // left out)
         float jk[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const float internal = (fp_scale * f[a] + fv_scale * f[3 + a]) * inv;
-            jk[a] = fmaf(-rate_i * inv, internal, (fp_scale * f[6 + a] + fv_scale * f[9 + a]) * inv);
+            const float pressure_acc = fp_scale * f[a] * inv;
+            jk[a] = fmaf(-rate_i * inv, pressure_acc, fp_scale * f[6 + a] * inv);
         }
         fb.out[ti] = make_float4(jk[0], jk[1], jk[2], rate_i);
     }
