@@ -329,7 +329,7 @@ def by_id(f) -> np.ndarray:
 
 
 def run_rollouts(p, st, dt, steps: int, K: int = 4, tolerance: float = 0.01, gnn_steps: int = 8,
-                 cycle_lengths=(4, 5)) -> dict:
+                 cycle_lengths=(4, 5, 6)) -> dict:
     """Rollouts of `steps` steps from `st`, each on a fresh fluid, against plain SPH over the same
     steps: cycles of one judge SPH step and K - 1 extrapolated steps in the three modes of the
     fast rollout: "learned" (a + k dt J plus the network's residual), "taylor" (a + k dt J) and

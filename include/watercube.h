@@ -540,7 +540,7 @@ WC_API wc_status wc_surrogate_rollout(wc_surrogate* s, wc_fluid* f, float dt, ui
 typedef struct wc_local wc_local;
 
 typedef struct wc_local_config {
-    uint32_t ages;        /* K - 1: predicted ages, 1 .. 4 */
+    uint32_t ages;        /* K - 1: predicted ages, 1 .. 5 */
     uint32_t seed;        /* weight initialisation */
     float accel_scale;    /* accelerations are learned in units of this (m/s^2) */
     float velocity_scale; /* velocities enter in units of this (m/s) */
@@ -567,9 +567,9 @@ WC_API wc_status wc_local_train(wc_local* net, uint32_t steps, uint32_t rows, fl
 /* Test hook: the loss and the gradient of every parameter ([wc_local_num_params]) on the
    training samples with the given row indices (modulo the sample count), without an update. */
 WC_API wc_status wc_local_gradients(wc_local* net, const uint32_t* rows_idx, uint32_t rows, float* grads, float* loss);
-/* Copy samples [first, first + count) of a set: inputs [count][32] and targets [count][16]:
+/* Copy samples [first, first + count) of a set: inputs [count][32] and targets [count][20]:
    columns 3 (k - 1) .. + 2 the residual (a(t + k) - a(t) - k dt J) / accel_scale of age k,
-   column 12 (1 ms / dt)^2 (the residuals' factor into the network's units), columns 13 .. 15
+   column 16 (1 ms / dt)^2 (the residuals' factor into the network's units), columns 17 .. 19
    dt J / accel_scale; either pointer may be NULL. */
 WC_API wc_status wc_local_get_samples(wc_local* net, int held_out, uint64_t first, uint64_t count, float* inputs,
                                       float* targets);

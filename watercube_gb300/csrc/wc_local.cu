@@ -51,7 +51,13 @@ using namespace wc;
 
 namespace {
 
-constexpr uint32_t IN = 32, IN_USED = 19, HID = 64, OUT = 16, MAX_AGES = 4;
+constexpr uint32_t IN = 32, IN_USED = 19, HID = 64, OUT = 16, MAX_AGES = 5;
+// A sample's targets: YW floats, the residuals of ages 1 .. MAX_AGES in columns 0 .. 3 MAX_AGES - 1,
+// then (DT_REF / dt)^2 in column RES_SCALE and dt J / a_s in columns JD .. JD + 2.
+constexpr uint32_t YW = 20, RES_SCALE = 16, JD = 17;
+// The network's changes per particle in a rollout: 3 MAX_AGES columns padded to 16 (whole 16-byte stores).
+constexpr uint32_t CHANGE_LD = 16;
+static_assert(3 * MAX_AGES <= OUT && 3 * MAX_AGES <= RES_SCALE && 3 * MAX_AGES <= CHANGE_LD, "ages do not fit");
 constexpr uint32_t TILE = 128;
 constexpr uint32_t MLP_THREADS = 128;
 constexpr uint32_t MLP_CTAS_PER_SM = 6;
@@ -63,7 +69,6 @@ constexpr uint32_t WAIT_LIMIT = 1u << 22;
 // a_s (dt / DT_REF)^2 (the residual grows with the square of the time step), so that one network
 // serves every dt. Column RES_SCALE of a sample's targets holds (DT_REF / dt)^2.
 constexpr float DT_REF = 1e-3f;
-constexpr uint32_t RES_SCALE = 12;
 
 // FP32 master parameters, W as [k_in x n_out] row-major (the convention of cast_weight).
 constexpr size_t OFF_W1 = 0;
@@ -215,8 +220,8 @@ __device__ __forceinline__ void skip_particle(const SceneConsts& c, float dt, ui
 // the judge step's sorted order), the judge step's acceleration and features, and the slot that
 // keeps the state after the judge step for a revert.
 struct SkipArgs {
-    float4 *pos, *vel;
-    const float4 *acc, *feat, *pos_b;  // pos_b.w: the judge step's SPH density (rho_t)
+    float4 *pos, *vel;  // pos.w after the judge step: its SPH density (rho_t)
+    const float4 *acc, *feat;
     float4 *save_pos, *save_vel;
     const uint32_t* ids;
     uint32_t* save_ids;
@@ -250,7 +255,7 @@ __global__ void skip_cycle_kernel(uint32_t n, const SceneConsts sc0, const Batch
         if (change && j < 3u * k.ages) x += change[(size_t)i * ldc + j] - mean[j];
         ch[j] = x;
     }
-    skip_particle(c, k.dt, k.ages, k.acc[i], (change || k.taylor) ? ch : nullptr, k.pos_b[i].w, jf.w, p, v);
+    skip_particle(c, k.dt, k.ages, k.acc[i], (change || k.taylor) ? ch : nullptr, p.w, jf.w, p, v);
     k.pos[i] = p;
     k.vel[i] = v;
 }
@@ -597,7 +602,7 @@ __global__ void __launch_bounds__(JUDGE_THREADS) judge_final_kernel(uint32_t chu
 // ---- sample recording ---------------------------------------------------------------------------
 
 // a0_by_id[ids[i]] = acc[i]
-// The judge step's acceleration and J by particle id; y_by_id[id][13 .. 15] = dt J / a_s and
+// The judge step's acceleration and J by particle id; y_by_id[id][JD .. JD + 2] = dt J / a_s and
 // y_by_id[id][RES_SCALE] = (DT_REF / dt)^2.
 __global__ void scatter_judge_kernel(uint32_t n, const uint32_t* __restrict__ ids, const float4* __restrict__ acc,
                                      const float4* __restrict__ feat, float dt, float inv_a,
@@ -609,11 +614,11 @@ __global__ void scatter_judge_kernel(uint32_t n, const uint32_t* __restrict__ id
     const float4 j = feat[i];
     a0_by_id[id] = acc[i];
     j0_by_id[id] = j;
-    float* y = y_by_id + (size_t)id * OUT;
+    float* y = y_by_id + (size_t)id * YW;
     y[RES_SCALE] = (DT_REF / dt) * (DT_REF / dt);
-    y[13] = j.x * dt * inv_a;
-    y[14] = j.y * dt * inv_a;
-    y[15] = j.z * dt * inv_a;
+    y[JD] = j.x * dt * inv_a;
+    y[JD + 1] = j.y * dt * inv_a;
+    y[JD + 2] = j.z * dt * inv_a;
 }
 // y_by_id[ids[i]][3 (age - 1) ..] = (acc[i] - a0 - age dt J) * inv_a: the residual of the Taylor
 // extrapolation the network learns.
@@ -625,7 +630,7 @@ __global__ void target_kernel(uint32_t n, const uint32_t* __restrict__ ids, cons
     const uint32_t id = ids[i];
     const float4 a = acc[i], b = a0_by_id[id], j = j0_by_id[id];
     const float kdt = (float)age * dt;
-    float* y = y_by_id + (size_t)id * OUT + 3u * (age - 1u);
+    float* y = y_by_id + (size_t)id * YW + 3u * (age - 1u);
     y[0] = (a.x - fmaf(kdt, j.x, b.x)) * inv_a;
     y[1] = (a.y - fmaf(kdt, j.y, b.y)) * inv_a;
     y[2] = (a.z - fmaf(kdt, j.z, b.z)) * inv_a;
@@ -657,11 +662,11 @@ __global__ void gather_rows_kernel(uint32_t rows, uint64_t seed, uint64_t count,
 #pragma unroll
     for (int q = 0; q < (int)IN / 8; ++q) dx[q] = sx[q];
     // the residuals in the network's units: times (DT_REF / dt)^2 (column RES_SCALE)
-    const float* sy = ys + k * OUT;
+    const float* sy = ys + k * YW;
     const float sc = sy[RES_SCALE];
     float* dy = yb + (size_t)r * OUT;
 #pragma unroll
-    for (int q = 0; q < (int)OUT; ++q) dy[q] = q < (int)RES_SCALE ? sy[q] * sc : 0.f;
+    for (int q = 0; q < (int)OUT; ++q) dy[q] = q < (int)(3 * MAX_AGES) ? sy[q] * sc : 0.f;
 }
 
 // Mean squared error over the used outputs: d = 2 (p - t) / (rows nout) (FP32 and BF16, unused
@@ -706,7 +711,7 @@ __global__ void reduce_splits_kernel(uint32_t count, uint32_t splits, const floa
 }
 
 // Evaluation sums per age k (units of a_s; y the residual, jd = dt J from the targets' columns
-// 13 .. 15, a0 from the inputs' first three columns, pred converted from the network's units):
+// JD .., a0 from the inputs' first three columns, pred converted from the network's units):
 // |pred - y|^2 (network mode),
 // |y + k jd|^2 (stale mode), |y|^2 (Taylor mode), |a0 + y + k jd|^2 (the acceleration).
 constexpr uint32_t EVAL_SUMS = 4;
@@ -723,9 +728,9 @@ __global__ void eval_kernel(uint64_t rows, uint32_t ages, const __nv_bfloat16* _
         for (uint32_t g = 0; g < ages; ++g) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const double y = ys[r * OUT + 3 * g + c];
-                const double p = pred[r * OUT + 3 * g + c] / (double)ys[r * OUT + RES_SCALE];
-                const double ch = y + (double)(g + 1) * ys[r * OUT + 13 + c];
+                const double y = ys[r * YW + 3 * g + c];
+                const double p = pred[r * OUT + 3 * g + c] / (double)ys[r * YW + RES_SCALE];
+                const double ch = y + (double)(g + 1) * ys[r * YW + JD + c];
                 const double t = a0[c] + ch;
                 acc[EVAL_SUMS * g + 0] += (p - y) * (p - y);
                 acc[EVAL_SUMS * g + 1] += ch * ch;
@@ -970,7 +975,7 @@ wc_status ensure_n(wc_local* s, uint32_t n) {
     dfree(s->vxyz);
     s->cap_n = 0;
     WC_TRY(dalloc(&s->x_id, (size_t)n * IN));
-    WC_TRY(dalloc(&s->y_id, (size_t)n * OUT));
+    WC_TRY(dalloc(&s->y_id, (size_t)n * YW));
     WC_TRY(dalloc(&s->a0_id, n));
     WC_TRY(dalloc(&s->j0_id, n));
     WC_TRY(dalloc(&s->feat, n));
@@ -984,7 +989,7 @@ wc_status ensure_samples(wc_local* s, int set) {
     if (s->xs[set]) return WC_OK;
     const uint64_t cap = set == 0 ? s->cfg.capacity : std::max<uint64_t>(s->cfg.capacity / 4, 1);
     WC_TRY(dalloc(&s->xs[set], cap * IN));
-    WC_TRY(dalloc(&s->ys[set], cap * OUT));
+    WC_TRY(dalloc(&s->ys[set], cap * YW));
     s->cap[set] = cap;
     s->count[set] = 0;
     return WC_OK;
@@ -1013,7 +1018,7 @@ wc_status record(wc_local* s, const StepTarget& t0, float dt, uint32_t cycles, i
                 inputs_kernel<true><<<blocks_for(n, 128), 128, 0, t.stream>>>(n, src, t.d->ids_b, s->x_id);
             else
                 inputs_kernel<false><<<blocks_for(n, 128), 128, 0, t.stream>>>(n, src, t.d->ids_b, s->x_id);
-            cudaMemsetAsync(s->y_id, 0, sizeof(float) * (size_t)n * OUT, t.stream);
+            cudaMemsetAsync(s->y_id, 0, sizeof(float) * (size_t)n * YW, t.stream);
             scatter_judge_kernel<<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.d->ids_a, t.d->accel, s->feat, dt,
                                                                           fs.inv_a, s->a0_id, s->j0_id, s->y_id);
         }
@@ -1032,7 +1037,7 @@ wc_status record(wc_local* s, const StepTarget& t0, float dt, uint32_t cycles, i
                  ? WC_OK
                  : fail(WC_ERR_CUDA, "sample copy failed");
         if (rc == WC_OK)
-            rc = cudaMemcpyAsync(s->ys[set] + base * OUT, s->y_id, sizeof(float) * (size_t)n * OUT,
+            rc = cudaMemcpyAsync(s->ys[set] + base * YW, s->y_id, sizeof(float) * (size_t)n * YW,
                                  cudaMemcpyDeviceToDevice, t.stream) == cudaSuccess
                      ? WC_OK
                      : fail(WC_ERR_CUDA, "sample copy failed");
@@ -1205,7 +1210,7 @@ wc_status ensure_roll(wc_local* s, uint32_t n) {
         dfree(s->save_ids[q]);
     }
     s->cap_roll = 0;
-    WC_TRY(dalloc(&s->change, (size_t)n * 3u * MAX_AGES));
+    WC_TRY(dalloc(&s->change, (size_t)n * CHANGE_LD));
     if (!s->mean_part) WC_TRY(dalloc(&s->mean_part, (size_t)s->sms * MLP_CTAS_PER_SM * OUT));
     if (!s->mean) WC_TRY(dalloc(&s->mean, OUT));
     WC_TRY(dalloc(&s->judge_part, blocks_for(n, 32)));
@@ -1391,7 +1396,7 @@ WC_API wc_status wc_local_get_samples(wc_local* s, int held_out, uint64_t first,
         for (size_t i = 0; i < h.size(); ++i) inputs[i] = __bfloat162float(h[i]);
     }
     if (targets) {
-        WC_CUDA_TRY(cudaMemcpyAsync(targets, s->ys[set] + first * OUT, sizeof(float) * (size_t)count * OUT,
+        WC_CUDA_TRY(cudaMemcpyAsync(targets, s->ys[set] + first * YW, sizeof(float) * (size_t)count * YW,
                                     cudaMemcpyDeviceToHost, s->stream));
         WC_CUDA_TRY(cudaStreamSynchronize(s->stream));
     }
@@ -1551,7 +1556,7 @@ WC_API wc_status wc_local_rollout_mode(wc_local* s, wc_fluid* f, float dt, uint3
     // kernel (the network's, or the stale acceleration's); the judge state goes to save slot `slot`.
     auto skip_steps = [&](uint32_t count, int slot) {
         if (!n || !count) return;
-        SkipArgs k{d.pos_a, d.vel_a, d.accel, w->feat, d.pos_b, w->save_pos[slot], w->save_vel[slot],
+        SkipArgs k{d.pos_a, d.vel_a, d.accel, w->feat, w->save_pos[slot], w->save_vel[slot],
                    ids ? d.ids_a : nullptr, w->save_ids[slot], dt, count, taylor};
         if (net) {
             // the network's residuals and their mean over the particles, then the skipped steps
@@ -1559,11 +1564,11 @@ WC_API wc_status wc_local_rollout_mode(wc_local* s, wc_fluid* f, float dt, uint3
             const InputSrc src = input_src(net, t, dt);
             const int grid = mlp_grid(net, n);
             mlp_kernel<true, false, true><<<grid, MLP_THREADS, 0, t.stream>>>(
-                n, src, nullptr, weights(net), w->change, 3u * MAX_AGES, 3u * MAX_AGES, residual_scale(net, dt), net->d_err,
-                w->mean_part);  // all 3 MAX_AGES columns (whole 16-byte stores); the skipped steps read 3 count
+                n, src, nullptr, weights(net), w->change, CHANGE_LD, CHANGE_LD, residual_scale(net, dt), net->d_err,
+                w->mean_part);  // all CHANGE_LD columns (whole 16-byte stores); the skipped steps read 3 count
             output_mean_kernel<<<1, 32 * OUT, 0, t.stream>>>((uint32_t)grid, n, w->mean_part, w->mean);
             skip_cycle_kernel<false><<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.sc, BatchTables{}, k, w->change,
-                                                                               3u * MAX_AGES, w->mean);
+                                                                               CHANGE_LD, w->mean);
         } else {
             skip_cycle_kernel<false><<<blocks_for(n, 256), 256, 0, t.stream>>>(n, t.sc, BatchTables{}, k, nullptr, 0,
                                                                                nullptr);

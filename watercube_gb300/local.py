@@ -22,6 +22,7 @@ from .batch import Batch
 from .fluid import Fluid
 
 IN, HIDDEN, OUT = 32, 64, 16
+YW = 20  # a sample's target row: residuals of 5 ages, unused, (1 ms / dt)^2, dt J / a_s
 INPUT_NAMES = ["a_x", "a_y", "a_z", "jdt_x", "jdt_y", "jdt_z", "rhodot", "v_x", "v_y", "v_z", "rho_rel", "p_rel",
                "wall_x0", "wall_x1", "wall_y0", "wall_y1", "wall_z0", "wall_z1", "k_rel"]
 DEFAULT_WEIGHTS = Path(__file__).resolve().parent / "weights" / "local_k4.npz"
@@ -76,7 +77,7 @@ class LocalNet:
         if count is None:
             count = self.num_samples(held_out) - first
         x = np.zeros((count, IN), np.float32)
-        y = np.zeros((count, OUT), np.float32)
+        y = np.zeros((count, YW), np.float32)
         check(lib().wc_local_get_samples(self._h, int(held_out), first, count, A._ptr(x), A._ptr(y)),
               "wc_local_get_samples")
         return x, y
