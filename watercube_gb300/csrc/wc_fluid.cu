@@ -211,7 +211,7 @@ wc_status launch_step(wc_fluid* f, const StepInputs& in) {
 }
 
 wc_status read_device_errors(wc_fluid* f) {
-    WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
+    // the copy follows everything already on the stream: one wait covers both
     WC_CUDA_TRY(cudaMemcpyAsync(f->h_err, f->d.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, f->stream));
     WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
     const uint32_t e = *f->h_err;
@@ -232,6 +232,10 @@ wc_status require(const wc_fluid* f, bool need_setup) {
     if (!f) return fail(WC_ERR_INVALID_ARG, "null fluid handle");
     if (need_setup && !f->setup_done) return fail(WC_ERR_STATE, "wc_fluid_setup has not been called");
     return WC_OK;
+}
+
+__global__ void iota_kernel(uint32_t* __restrict__ out, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = i;
 }
 
 }  // namespace
@@ -401,8 +405,8 @@ WC_API wc_status wc_fluid_get_particles(wc_fluid* f, int buffer, wc_particle* ou
     if (n != f->d.n) return fail(WC_ERR_INVALID_ARG, "copy of %u particles, handle holds %u", n, f->d.n);
     if (!n) return read_device_errors(f);
     if (!out) return fail(WC_ERR_INVALID_ARG, "null output");
-    WC_TRY(ensure_staging(f));
     const bool st = buffer == WC_BUFFER_STATE;
+    WC_TRY(ensure_staging(f));
     launch_soa_to_aos(st ? f->d.pos_a : f->d.pos_b, st ? f->d.vel_a : f->d.vel_b, f->staging, n, f->stream);
     WC_TRY(check_launch());
     WC_CUDA_TRY(cudaMemcpyAsync(out, f->staging, sizeof(wc_particle) * (size_t)n, cudaMemcpyDeviceToHost, f->stream));
@@ -418,16 +422,15 @@ WC_API wc_status wc_fluid_set_particles(wc_fluid* f, int buffer, const wc_partic
     if (n != f->d.n) return fail(WC_ERR_INVALID_ARG, "copy of %u particles, handle holds %u", n, f->d.n);
     if (!n) return WC_OK;
     if (!in) return fail(WC_ERR_INVALID_ARG, "null input");
+    const bool st = buffer == WC_BUFFER_STATE;
     WC_TRY(ensure_staging(f));
     WC_CUDA_TRY(cudaMemcpyAsync(f->staging, in, sizeof(wc_particle) * (size_t)n, cudaMemcpyHostToDevice, f->stream));
-    const bool st = buffer == WC_BUFFER_STATE;
     launch_aos_to_soa(f->staging, st ? f->d.pos_a : f->d.pos_b, st ? f->d.vel_a : f->d.vel_b, n, f->stream);
     WC_TRY(check_launch());
     if (st && f->d.ids_a) {
         // tracked ids restart at the uploaded order
-        std::vector<uint32_t> iota(n);
-        for (uint32_t i = 0; i < n; ++i) iota[i] = i;
-        WC_CUDA_TRY(cudaMemcpyAsync(f->d.ids_a, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, f->stream));
+        iota_kernel<<<(n + 1023) / 1024, 256, 0, f->stream>>>(f->d.ids_a, n);
+        WC_TRY(check_launch());
     }
     // The host buffer may be reused as soon as this returns.
     WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
