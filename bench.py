@@ -1,7 +1,8 @@
 """Benchmark of the plain SPH step at 1,048,576 particles (the dam break the solver is measured
 on), printing one JSON line.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload dam1m|dam16k]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload dam1m|dam16k|batch512|rollout1m]
 
 value      particle-steps/s of K graph-launched steps (the timed window: steps W+1 .. W+K of the
            workload from its initial state), inputs resident in HBM, device time from CUDA events
@@ -20,11 +21,15 @@ cpu_baseline  the CPU transcription of the reference's stages (oracle, FP32) on 
 surface    surface extraction of the same state: colour field on 256^3 vertices and marching
            cubes, CUDA-event times.
 rollout    rollouts at the same size from the same initial state, --rollout-steps steps each:
-           plain SPH, the learned fast rollout (a judge SPH step every K = 4 steps, the network
-           predicting the skipped steps' accelerations) and the same cycles on the stale SPH
-           acceleration (the method without the network), with the judge's density error and
-           the position drift from plain SPH; the message-passing network's modes a few steps
-           each. `--workload rollout1m` times them alone with --steps steps (default 2,000).
+           plain SPH and the fast rollout's three modes (a judge SPH step every K steps, the
+           K - 1 steps between on the judge's acceleration extrapolated to first order plus the
+           network's residual ("learned"), to first order ("taylor"), or held ("stale")) for
+           K = 4 and every other K with trained weights (5, 6), with the judge's density error
+           and the position drift from plain SPH; the message-passing network's modes a few
+           steps each. `--workload rollout1m` times them alone with --steps steps (default
+           2,000) and reports the fastest learned mode within the density tolerance.
+--workload batch512  512 scenes of 4,096-65,536 particles in one launch per stage, 500 steps
+           after the autotuner (its choice in `tuning`).
 Multi-GPU (torchrun): every rank runs an independent replica (the path has no exchange step);
 the slowest rank's time is reported.
 """
