@@ -9,7 +9,9 @@ value      particle-steps/s of K graph-launched steps (the timed window: steps W
            around each step; L2 is flushed (a read of twice its size) before every timed step,
            outside the timed span.
 e2e        the same metric over the same window through the C ABI with host buffers: each step
-           uploads the particle state from pinned host memory, runs update(), and reads it back.
+           is one wc_fluid_update_host call, which uploads the particle state from pinned host
+           memory, runs the step and reads the state back (each eighth of the slots copied out
+           as soon as the force pass has stored it, while the pass computes the rest).
 roofline   the dominant kernel's algorithmic bytes per launch / its mean CUDA-event time over the
            same window (separately launched kernels), against the measured HBM copy bandwidth;
            `traffic` is its DRAM bytes per launch from ncu (profiles/ncu_traffic.json).
@@ -566,9 +568,7 @@ def run_ours(args):
     e2e_steps = args.steps  # the same window as the device-timed steps
 
     def e2e_step(src, dst):
-        _abi.check(lib.wc_fluid_set_particles(f._handle, _abi.WC_BUFFER_STATE, src.ctypes.data, n))
-        _abi.check(lib.wc_fluid_update(f._handle, dt / float(p.time_scale)))
-        _abi.check(lib.wc_fluid_get_particles(f._handle, _abi.WC_BUFFER_STATE, dst.ctypes.data, n))
+        _abi.check(lib.wc_fluid_update_host(f._handle, dt / float(p.time_scale), src.ctypes.data, dst.ctypes.data, n))
 
     for _ in range(2):
         e2e_step(ain, aout)
@@ -616,7 +616,8 @@ def run_ours(args):
         "kernels_ms": kmean,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps,
-                "pattern": "wc_fluid_set_particles(pinned host) + wc_fluid_update + wc_fluid_get_particles(pinned host)"},
+                "pattern": "wc_fluid_update_host(pinned host in, pinned host out): upload, step, readback "
+                           "overlapping the force pass"},
         "gpu_launches": 6 * args.steps,
         "clocks": clock_summary,
     }

@@ -226,6 +226,18 @@ WC_API wc_status wc_fluid_get_particles(wc_fluid* f, int buffer, wc_particle* ou
 /* util::setParticles (util.cpp:74-78): overwrite a buffer from host. With WC_FLAG_TRACK_IDS,
    writing the state buffer restarts the particle ids at the uploaded order (id = index). */
 WC_API wc_status wc_fluid_set_particles(wc_fluid* f, int buffer, const wc_particle* in, uint32_t n);
+
+/* One update with host buffers, the three calls a host-side caller makes per frame in one:
+   wc_fluid_set_particles(WC_BUFFER_STATE, in) (skipped when in is null), wc_fluid_update(time)
+   and wc_fluid_get_particles(WC_BUFFER_STATE, out) (skipped when out is null), with the same
+   results bit for bit. The readback overlaps the step: the force pass writes the host records
+   of the particles it stores and flags each eighth of the slots in mapped host memory once it
+   is complete, and the calling thread copies that part out while the pass computes the rest
+   (lane passes; with WC_FLAG_CELL_TEAMS the copy follows the step). Pinned host memory
+   (cudaMallocHost, wc_alloc_host) lets the copies run alongside; pageable memory gives the same
+   results without the overlap. Returns after the copy to out has landed (or, with out null,
+   like wc_fluid_update). */
+WC_API wc_status wc_fluid_update_host(wc_fluid* f, double time, const wc_particle* in, wc_particle* out, uint32_t n);
 /* util::getUints (util.cpp:62-72): synchronise and copy an integer buffer (WC_UINTS_*). n must
    equal its length: num_particles, or num_cells for the two cell tables. */
 WC_API wc_status wc_fluid_get_uints(wc_fluid* f, int which, uint32_t* out, size_t n);

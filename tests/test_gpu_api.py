@@ -80,6 +80,59 @@ def test_pinned_host_copies_round_trip(gpu):
         hout.free()
 
 
+@pytest.mark.parametrize("flags", [0, _abi.WC_FLAG_CELL_TEAMS, _abi.WC_FLAG_TRACK_IDS])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_update_host_equals_the_three_calls(gpu, flags, pinned):
+    """wc_fluid_update_host(time, in, out) = set_particles(in) + update(time) + particles(), bit
+    for bit, whether the readback overlaps the force pass (lane passes: parts flagged by the
+    pass) or follows the step (cell teams), into pageable or pinned memory; without `in` it
+    steps the device state, without `out` it reads nothing back. The 1M case has parts of many
+    chunks, the 16k case parts of a few."""
+    from watercube_gb300.fluid import PinnedBuffer
+
+    for name in ("dam16k", "dam1m"):
+        p, st = case(name, flags)
+        n = st.shape[0]
+        bufs = [PinnedBuffer(32 * n), PinnedBuffer(32 * n)] if pinned else []
+        try:
+            a_in = bufs[0].particles(n) if pinned else np.empty(n, st.dtype)
+            a_out = bufs[1].particles(n) if pinned else np.empty(n, st.dtype)
+            with fluid(p, st) as a, fluid(p, st) as b:
+                a_in[:] = st
+                for k in range(4):
+                    if k == 2:
+                        a.update_host(1.0 / 60.0, None, a_out)  # the device state as it is
+                        b.update(1.0 / 60.0)
+                    elif k == 3:
+                        a.update_host(1.0 / 60.0, a_in, None)  # no readback
+                        b.set_particles(a_in)
+                        b.update(1.0 / 60.0)
+                        a_out[:] = a.particles()
+                    else:
+                        a.update_host(1.0 / 60.0, a_in, a_out)
+                        b.set_particles(a_in)
+                        b.update(1.0 / 60.0)
+                    ref = b.particles()
+                    assert a_out.tobytes() == ref.tobytes(), (name, k)
+                    a_in[:] = a_out
+                    a_in["velocity"] *= 0.5  # an input that differs from the device state
+                assert a.step_count == b.step_count == 4
+                if flags & _abi.WC_FLAG_TRACK_IDS:
+                    assert np.array_equal(a.particle_ids(), b.particle_ids())
+        finally:
+            for buf in bufs:
+                buf.free()
+
+
+def test_update_host_checks_its_arguments(gpu):
+    p, st = case("dam16k")
+    with fluid(p, st) as f:
+        lib = _abi.lib()
+        assert lib.wc_fluid_update_host(f._handle, 1e-3, None, None, st.shape[0] - 1) == _abi.WC_ERR_INVALID_ARG
+        with pytest.raises(ValueError):
+            f.update_host(1e-3, st[:-1], None)
+
+
 def test_set_particles_restarts_tracked_ids(gpu):
     p, st = case("dam16k", _abi.WC_FLAG_TRACK_IDS)
     with fluid(p, st) as f:

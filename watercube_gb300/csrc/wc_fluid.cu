@@ -3,6 +3,7 @@
 // six kernels of a step on its own stream, and replays them as one CUDA graph per update.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -19,6 +20,11 @@ const char* const STEP_KERNEL_NAMES[NUM_STEP_KERNELS] = {"bin_count", "scan_cell
                                                          "rank_gather", "density", "force_integrate"};
 
 bool same_inputs(const StepInputs& a, const StepInputs& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
+
+// wc_fluid_update_host copies the state out in READBACK_PARTS parts of consecutive slots, each
+// as soon as the force pass has stored it (the pass flags it in mapped host memory), while the
+// pass computes the rest; only the last part's copy follows the pass.
+constexpr uint32_t READBACK_PARTS = 8;
 
 }  // namespace
 
@@ -42,6 +48,13 @@ struct wc_fluid {
     // host-copy staging (AoS, 32 bytes per particle) and error word
     float4* staging = nullptr;
     uint32_t* h_err = nullptr;
+    // wc_fluid_update_host (created on first use): the readback's copy stream, the force pass's
+    // per-part chunk counters (device) and part flags (mapped host memory), the call counter
+    cudaStream_t copy_stream = nullptr;
+    uint32_t* part_done = nullptr;
+    uint32_t* part_flag = nullptr;
+    uint32_t* part_flag_dev = nullptr;
+    uint32_t readback_seq = 0;
     // L2 flush for timing
     float4* flush_buf = nullptr;
     size_t flush_n4 = 0;
@@ -69,6 +82,9 @@ void free_all(wc_fluid* f) {
     if (f->h_err) cudaFreeHost(f->h_err);
     if (f->exec) cudaGraphExecDestroy(f->exec);
     if (f->graph) cudaGraphDestroy(f->graph);
+    if (f->part_done) cudaFree(f->part_done);
+    if (f->part_flag) cudaFreeHost(f->part_flag);
+    if (f->copy_stream) cudaStreamDestroy(f->copy_stream);
     if (f->stream) cudaStreamDestroy(f->stream);
 }
 
@@ -124,6 +140,24 @@ wc_status allocate(wc_fluid* f) {
 
 wc_status ensure_staging(wc_fluid* f) {
     if (!f->staging && f->d.n) WC_TRY(dalloc(&f->staging, 2 * (size_t)f->d.n));
+    return WC_OK;
+}
+
+__global__ void iota_kernel(uint32_t* __restrict__ out, uint32_t n);
+wc_status check_launch();
+
+// Host AoS -> the state (or sorted) buffer, on the fluid's stream, without waiting: the caller
+// waits before the host buffer may change.
+wc_status enqueue_upload(wc_fluid* f, bool state, const wc_particle* in, uint32_t n) {
+    WC_TRY(ensure_staging(f));
+    WC_CUDA_TRY(cudaMemcpyAsync(f->staging, in, sizeof(wc_particle) * (size_t)n, cudaMemcpyHostToDevice, f->stream));
+    launch_aos_to_soa(f->staging, state ? f->d.pos_a : f->d.pos_b, state ? f->d.vel_a : f->d.vel_b, n, f->stream);
+    WC_TRY(check_launch());
+    if (state && f->d.ids_a) {
+        // tracked ids restart at the uploaded order
+        iota_kernel<<<(n + 1023) / 1024, 256, 0, f->stream>>>(f->d.ids_a, n);
+        WC_TRY(check_launch());
+    }
     return WC_OK;
 }
 
@@ -422,19 +456,66 @@ WC_API wc_status wc_fluid_set_particles(wc_fluid* f, int buffer, const wc_partic
     if (n != f->d.n) return fail(WC_ERR_INVALID_ARG, "copy of %u particles, handle holds %u", n, f->d.n);
     if (!n) return WC_OK;
     if (!in) return fail(WC_ERR_INVALID_ARG, "null input");
-    const bool st = buffer == WC_BUFFER_STATE;
-    WC_TRY(ensure_staging(f));
-    WC_CUDA_TRY(cudaMemcpyAsync(f->staging, in, sizeof(wc_particle) * (size_t)n, cudaMemcpyHostToDevice, f->stream));
-    launch_aos_to_soa(f->staging, st ? f->d.pos_a : f->d.pos_b, st ? f->d.vel_a : f->d.vel_b, n, f->stream);
-    WC_TRY(check_launch());
-    if (st && f->d.ids_a) {
-        // tracked ids restart at the uploaded order
-        iota_kernel<<<(n + 1023) / 1024, 256, 0, f->stream>>>(f->d.ids_a, n);
-        WC_TRY(check_launch());
-    }
+    WC_TRY(enqueue_upload(f, buffer == WC_BUFFER_STATE, in, n));
     // The host buffer may be reused as soon as this returns.
     WC_CUDA_TRY(cudaStreamSynchronize(f->stream));
     return WC_OK;
+}
+
+WC_API wc_status wc_fluid_update_host(wc_fluid* f, double time, const wc_particle* in, wc_particle* out, uint32_t n) {
+    clear_error();
+    WC_NVTX("wc_fluid_update_host");
+    WC_TRY(require(f, true));
+    if (n != f->d.n) return fail(WC_ERR_INVALID_ARG, "copy of %u particles, handle holds %u", n, f->d.n);
+    if (!n || !out || f->ld.pass_variant != PASSES_LANE) {
+        // nothing to overlap: the three calls in turn
+        if (n && in) WC_TRY(wc_fluid_set_particles(f, WC_BUFFER_STATE, in, n));
+        WC_TRY(wc_fluid_update(f, time));
+        return out ? wc_fluid_get_particles(f, WC_BUFFER_STATE, out, n) : WC_OK;
+    }
+    f->in.dt = (float)time * f->params.time_scale;  // Fluid.cpp:308
+    if (in) WC_TRY(enqueue_upload(f, true, in, n));  // the final wait covers the copy from in
+    WC_TRY(ensure_staging(f));
+    if (!f->copy_stream) WC_CUDA_TRY(cudaStreamCreateWithFlags(&f->copy_stream, cudaStreamNonBlocking));
+    if (!f->part_done) {
+        WC_TRY(dalloc(&f->part_done, READBACK_PARTS));
+        WC_CUDA_TRY(cudaMemsetAsync(f->part_done, 0, sizeof(uint32_t) * READBACK_PARTS, f->stream));
+    }
+    if (!f->part_flag) {
+        WC_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&f->part_flag), sizeof(uint32_t) * READBACK_PARTS,
+                                  cudaHostAllocMapped));
+        std::memset(f->part_flag, 0, sizeof(uint32_t) * READBACK_PARTS);
+        WC_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&f->part_flag_dev), f->part_flag, 0));
+    }
+    if (++f->readback_seq == 0) ++f->readback_seq;  // flags start at 0: never publish 0
+    const uint32_t seq = f->readback_seq;
+    const uint32_t chunks = (n + 31u) >> 5;
+    const uint32_t part_chunks = (chunks + READBACK_PARTS - 1) / READBACK_PARTS;
+    const uint32_t parts = (chunks + part_chunks - 1) / part_chunks;
+    StepInputs step = f->in;
+    step.aos_out = f->staging;  // the pass writes the host records itself: no conversion kernel
+    step.part_done = f->part_done;
+    step.part_flag = f->part_flag_dev;
+    step.part_chunks = part_chunks;
+    step.seq = seq;
+    // the step of the graph, launched directly with the readback fields
+    enqueue_sort(f);
+    launch_density(f->d, f->sc, f->ld, f->stream);
+    launch_force(f->d, f->sc, step, f->ld, f->stream);
+    WC_TRY(check_launch());
+    const volatile uint32_t* flag = f->part_flag;
+    for (uint32_t r = 0; r < parts; ++r) {
+        // part r is published once its last chunk is stored; a stream that has ended (or failed)
+        // without the flag ends the wait too, and the copy then reads what the stream left
+        for (uint32_t spin = 1; flag[r] != seq; ++spin)
+            if ((spin & 1023u) == 0u && cudaStreamQuery(f->stream) != cudaErrorNotReady) break;
+        const uint32_t s0 = r * part_chunks * 32u, s1 = std::min((r + 1) * part_chunks * 32u, n);
+        WC_CUDA_TRY(cudaMemcpyAsync(out + s0, f->staging + 2 * (size_t)s0, sizeof(wc_particle) * (size_t)(s1 - s0),
+                                    cudaMemcpyDeviceToHost, f->copy_stream));
+    }
+    WC_CUDA_TRY(cudaStreamSynchronize(f->copy_stream));
+    ++f->steps;
+    return read_device_errors(f);
 }
 
 WC_API wc_status wc_fluid_get_uints(wc_fluid* f, int which, uint32_t* out, size_t n) {

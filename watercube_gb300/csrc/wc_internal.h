@@ -111,6 +111,17 @@ struct StepInputs {
     float dt;
     float g[3];
     float mouse_o[3], mouse_d[3];
+    // A readback that overlaps the lane force pass (all null/zero otherwise): the pass also
+    // writes every particle it stores as the host's AoS record into aos_out (two float4 per
+    // slot), and the state's chunks of 32 slots form parts of part_chunks chunks; the warp that
+    // finishes the last chunk of part r puts part_done[r] (device counters, zero between
+    // launches) back to zero and writes seq to part_flag[r] (mapped host memory the host polls
+    // before it copies the part out).
+    float4* aos_out;
+    uint32_t* part_done;
+    uint32_t* part_flag;
+    uint32_t part_chunks;
+    uint32_t seq;
 };
 
 // Decoupled look-back scan over the cell histogram.

@@ -97,7 +97,7 @@ SceneConsts make_scene_consts(const wc_params& p) {
 }
 
 StepInputs make_step_inputs(const wc_params& p, float dt) {
-    StepInputs s;
+    StepInputs s{};
     s.dt = dt;
     for (int a = 0; a < 3; ++a) {
         s.g[a] = p.gravity[a];

@@ -954,8 +954,13 @@ __device__ __forceinline__ void integrate_store(const SceneConsts& sc, const Ste
         v[a] = va;
         x[a] = xa;
     }
-    pos_a[ti] = make_float4(x[0], x[1], x[2], rho);
-    vel_a[ti] = make_float4(v[0], v[1], v[2], pressure);
+    const float4 pa = make_float4(x[0], x[1], x[2], rho), va = make_float4(v[0], v[1], v[2], pressure);
+    pos_a[ti] = pa;
+    vel_a[ti] = va;
+    if (in.aos_out) {
+        in.aos_out[2 * (size_t)ti] = pa;
+        in.aos_out[2 * (size_t)ti + 1] = va;
+    }
     if (ids_a) ids_a[ti] = ids_b[ti];
     if (accel) accel[ti] = make_float4(acc[0], acc[1], acc[2], 0.f);
     if (FEAT == FEAT_RATE) fb.out[ti] = make_float4(0.f, 0.f, 0.f, -6.f * sc.m * sc.c6 * f[6]);
@@ -1267,6 +1272,24 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
 
 constexpr uint32_t LANE_LIST = 32;  // neighbour slots a lane collects before evaluating them
 
+// Readback progress (StepInputs part fields): after chunk m every lane fences its stores, and the
+// warp that brings its part's count to the part's size publishes the part: the counter goes back
+// to zero (no chunk of the part is left in this launch) and, after a system-scope fence, the
+// host flag takes this launch's sequence number. No thread waits on anything.
+__device__ __forceinline__ void report_chunk(const StepInputs& in, uint32_t m, uint32_t M, uint32_t lane) {
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) {
+        const uint32_t r = m / in.part_chunks;
+        const uint32_t size = min(in.part_chunks, M - r * in.part_chunks);
+        if (atomicAdd(in.part_done + r, 1u) == size - 1u) {
+            in.part_done[r] = 0u;
+            __threadfence_system();
+            *reinterpret_cast<volatile uint32_t*>(in.part_flag + r) = in.seq;
+        }
+    }
+}
+
 // The row of candidate q (the last row whose first candidate is <= q) and its slot, from the row
 // starts P[0..8] (P[0] = 0, non-decreasing) and offsets D[r] = first slot of row r - P[r].
 __device__ __forceinline__ uint32_t slot_of(uint32_t q, const uint32_t P[9], const uint32_t D[9]) {
@@ -1386,6 +1409,10 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 2 : 3) force_
                 // not evaluated (see MAX_CELL_PARTICLES): the particle keeps its state, reported
                 pos_a[ti] = pi;
                 vel_a[ti] = vi;
+                if (in.aos_out) {
+                    in.aos_out[2 * (size_t)ti] = pi;
+                    in.aos_out[2 * (size_t)ti + 1] = vi;
+                }
                 if (ids_a) ids_a[ti] = ids_b[ti];
                 if (accel) accel[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (FEAT) fb.out[ti] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1394,6 +1421,7 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 2 : 3) force_
                 integrate_store<FEAT>(sc, in, pi, vi, f, ti, pos_a, vel_a, ids_b, ids_a, accel, fb, ri.x);
             }
         }
+        if (in.part_done) report_chunk(in, m, M, lane);
     }
     // the chunk counter returns to zero for the next launch (see release_counter)
     if (lane == 0 && m == M + gridDim.x * (uint32_t)WARPS - 1u) atomicExch(counter, 0u);

@@ -219,6 +219,20 @@ class Fluid:
         arr = np.ascontiguousarray(arr, dtype=A.PARTICLE_DTYPE)
         check(lib().wc_fluid_set_particles(self._require(), buffer, A._ptr(arr), arr.shape[0]), "set_particles")
 
+    def update_host(self, time: float, inp: np.ndarray | None = None, out: np.ndarray | None = None) -> None:
+        """set_particles(inp) (when given), update(time) and particles() into `out` (when given)
+        in one call, the readback overlapping the step (wc_fluid_update_host). Arrays of
+        PARTICLE_DTYPE with one row per particle; `out` in pinned memory (PinnedBuffer) lets
+        the copies overlap."""
+        n = self.numParticles()
+        for a, name in ((inp, "inp"), (out, "out")):
+            if a is not None and (a.dtype != A.PARTICLE_DTYPE or a.shape != (n,) or not a.flags.c_contiguous):
+                raise ValueError(f"{name} must be a contiguous array of {n} particles")
+        if out is not None and not out.flags.writeable:
+            raise ValueError("out must be writeable")
+        check(lib().wc_fluid_update_host(self._require(), float(time), A._ptr(inp) if inp is not None else None,
+                                         A._ptr(out) if out is not None else None, n), "wc_fluid_update_host")
+
     def uints(self, which: int) -> np.ndarray:
         n = self.num_cells if which in (A.WC_UINTS_CELL_COUNTS, A.WC_UINTS_CELL_OFFSETS) else self.numParticles()
         out = np.zeros(n, dtype=np.uint32)
