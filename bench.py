@@ -698,9 +698,7 @@ def run_batch(args):
     e2e_steps = min(args.steps, 100)
     t = time.perf_counter()
     for _ in range(e2e_steps):
-        _abi.check(lib.wc_batch_set_particles(b._h, ain.ctypes.data, n))
-        _abi.check(lib.wc_batch_step(b._h, dt, 1))
-        _abi.check(lib.wc_batch_get_particles(b._h, aout.ctypes.data, n))
+        _abi.check(lib.wc_batch_step_host(b._h, dt, ain.ctypes.data, aout.ctypes.data, n))
         ain, aout = aout, ain
     el = time.perf_counter() - t
     line = {
@@ -731,7 +729,8 @@ def run_batch(args):
                    "trials": tuning.trials, "tune_seconds": tune_s},
         "e2e": {"value": n * e2e_steps / el, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps,
-                "pattern": "wc_batch_set_particles(pinned host) + wc_batch_step + wc_batch_get_particles(pinned host)"},
+                "pattern": "wc_batch_step_host(pinned host in, pinned host out): upload, step, readback "
+                           "overlapping the force pass"},
         "gpu_launches": 6 * args.steps,
         "clocks": clocks.summary(),
         "mass_total": float(d[:, 0].sum()),

@@ -310,6 +310,10 @@ WC_API wc_status wc_batch_setup(wc_batch* b, const wc_particle* initial, uint64_
 WC_API wc_status wc_batch_step(wc_batch* b, float dt, uint32_t nsteps);
 WC_API wc_status wc_batch_get_particles(wc_batch* b, wc_particle* out, uint64_t total);
 WC_API wc_status wc_batch_set_particles(wc_batch* b, const wc_particle* in, uint64_t total);
+/* One step with host buffers, as wc_fluid_update_host: wc_batch_set_particles(in) (skipped when
+   in is null), wc_batch_step(dt, 1) and wc_batch_get_particles(out) (skipped when out is null),
+   the same results bit for bit, the readback overlapping the force pass (lane passes). */
+WC_API wc_status wc_batch_step_host(wc_batch* b, float dt, const wc_particle* in, wc_particle* out, uint64_t total);
 /* offsets[num_scenes + 1]: scene s owns slots [offsets[s], offsets[s+1]). */
 WC_API wc_status wc_batch_scene_offsets(const wc_batch* b, uint64_t* offsets);
 WC_API uint32_t wc_batch_num_scenes(const wc_batch* b);

@@ -34,6 +34,35 @@ def test_batch_equals_scenes_run_alone(gpu):
             assert b.scene(s, out).tobytes() == alone.tobytes(), f"scene {s}"
 
 
+@pytest.mark.parametrize("teams", [False, True])
+def test_step_host_equals_the_three_calls(gpu, teams):
+    """wc_batch_step_host(dt, in, out) = set_particles(in) + step(dt) + particles(), bit for bit,
+    with the readback overlapping the force pass (lane passes) or following the step (teams);
+    without `in` it steps the device state. 64 scenes: parts of many chunks across scenes."""
+    specs = batch_specs(64, 600, 6000, seed=11)
+    params = [scene_params(s) for s in specs]
+    states = [scene_particles(s, p) for s, p in zip(specs, params)]
+    with Batch(params, states) as a, Batch(params, states) as b:
+        for x in (a, b):
+            t = x.tuning()
+            t.pass_variant = _abi.WC_PASSES_TEAM if teams else _abi.WC_PASSES_LANE
+            x.set_tuning(t)
+        n = a.num_particles
+        cur = a.particles()
+        out = np.empty(n, cur.dtype)
+        for k in range(3):
+            if k == 1:
+                a.step_host(1e-3, None, out)
+                b.step(1e-3, 1)
+            else:
+                a.step_host(1e-3, cur, out)
+                b.set_particles(cur)
+                b.step(1e-3, 1)
+            assert out.tobytes() == b.particles().tobytes(), k
+            cur = out.copy()
+            cur["velocity"] *= 0.5
+
+
 def test_batch_diagnostics_fp64(gpu, oracle):
     _, params, states = small_batch(5, seed=8)
     with Batch(params, states) as b:

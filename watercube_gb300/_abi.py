@@ -247,6 +247,7 @@ def _declare(lib) -> None:
         "wc_fluid_get_particles": (S, [P, C.c_int, P, C.c_uint32]),
         "wc_fluid_set_particles": (S, [P, C.c_int, P, C.c_uint32]),
         "wc_fluid_update_host": (S, [P, C.c_double, P, P, C.c_uint32]),
+        "wc_batch_step_host": (S, [P, C.c_float, P, P, C.c_uint64]),
         "wc_fluid_get_uints": (S, [P, C.c_int, P, C.c_size_t]),
         "wc_fluid_get_params": (S, [P, pp]),
         "wc_fluid_get_device_buffers": (S, [P, C.POINTER(DeviceBuffers)]),

@@ -64,6 +64,18 @@ class Batch:
         state = np.ascontiguousarray(state, dtype=A.PARTICLE_DTYPE)
         check(lib().wc_batch_set_particles(self._h, A._ptr(state), state.shape[0]), "wc_batch_set_particles")
 
+    def step_host(self, dt: float, inp: np.ndarray | None = None, out: np.ndarray | None = None) -> None:
+        """set_particles(inp) (when given), one step and particles() into `out` (when given) in one
+        call, the readback overlapping the step (wc_batch_step_host)."""
+        n = self.num_particles
+        for a, name in ((inp, "inp"), (out, "out")):
+            if a is not None and (a.dtype != A.PARTICLE_DTYPE or a.shape != (n,) or not a.flags.c_contiguous):
+                raise ValueError(f"{name} must be a contiguous array of {n} particles")
+        if out is not None and not out.flags.writeable:
+            raise ValueError("out must be writeable")
+        check(lib().wc_batch_step_host(self._h, float(dt), A._ptr(inp) if inp is not None else None,
+                                       A._ptr(out) if out is not None else None, n), "wc_batch_step_host")
+
     def ids(self) -> np.ndarray:
         """Per state slot, the particle's index in the initial state (all scenes concatenated)."""
         out = np.zeros(self.num_particles, np.uint32)

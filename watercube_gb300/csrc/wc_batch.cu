@@ -121,6 +121,7 @@ struct wc_batch {
     StepInputs graph_in{};
     float4* staging = nullptr;
     uint32_t* h_err = nullptr;
+    HostReadback readback{};  // wc_batch_step_host
     float4* flush_buf = nullptr;
     size_t flush_n4 = 0;
     float* flush_sink = nullptr;
@@ -151,6 +152,7 @@ void free_batch(wc_batch* b) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->h_err) cudaFreeHost(b->h_err);
+    b->readback.release();
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -658,6 +660,34 @@ WC_API wc_status wc_batch_get_particles(wc_batch* b, wc_particle* out, uint64_t 
     WC_TRY(ensure_staging(b));
     launch_soa_to_aos(b->d.pos_a, b->d.vel_a, b->staging, (uint32_t)total, b->stream);
     WC_CUDA_TRY(cudaMemcpyAsync(out, b->staging, sizeof(wc_particle) * total, cudaMemcpyDeviceToHost, b->stream));
+    return read_errors(b);
+}
+
+WC_API wc_status wc_batch_step_host(wc_batch* b, float dt, const wc_particle* in, wc_particle* out, uint64_t total) {
+    clear_error();
+    WC_NVTX("wc_batch_step_host");
+    WC_TRY(require(b, true));
+    if (total != b->n) return fail(WC_ERR_INVALID_ARG, "%llu particles given, batch holds %llu",
+                                   (unsigned long long)total, (unsigned long long)b->n);
+    if (!total || !out || b->ld.pass_variant != PASSES_LANE) {
+        // nothing to overlap: the three calls in turn
+        if (total && in) WC_TRY(wc_batch_set_particles(b, in, total));
+        WC_TRY(wc_batch_step(b, dt, 1));
+        return out ? wc_batch_get_particles(b, out, total) : WC_OK;
+    }
+    const uint32_t n = (uint32_t)total;
+    b->in.dt = dt;
+    WC_TRY(ensure_staging(b));
+    if (in) {
+        // the final wait covers the copy from in
+        WC_CUDA_TRY(cudaMemcpyAsync(b->staging, in, sizeof(wc_particle) * total, cudaMemcpyHostToDevice, b->stream));
+        launch_aos_to_soa(b->staging, b->d.pos_a, b->d.vel_a, n, b->stream);
+    }
+    StepInputs step = b->in;
+    WC_TRY(b->readback.arm(b->stream, n, b->staging, step));
+    enqueue_step(b, step);  // the graph's stages, launched directly with the readback fields
+    WC_CUDA_TRY(cudaGetLastError());
+    WC_TRY(b->readback.drain(b->stream, n, b->staging, out));
     return read_errors(b);
 }
 

@@ -21,10 +21,6 @@ const char* const STEP_KERNEL_NAMES[NUM_STEP_KERNELS] = {"bin_count", "scan_cell
 
 bool same_inputs(const StepInputs& a, const StepInputs& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
 
-// wc_fluid_update_host copies the state out in READBACK_PARTS parts of consecutive slots, each
-// as soon as the force pass has stored it (the pass flags it in mapped host memory), while the
-// pass computes the rest; only the last part's copy follows the pass.
-constexpr uint32_t READBACK_PARTS = 8;
 
 }  // namespace
 
@@ -48,13 +44,7 @@ struct wc_fluid {
     // host-copy staging (AoS, 32 bytes per particle) and error word
     float4* staging = nullptr;
     uint32_t* h_err = nullptr;
-    // wc_fluid_update_host (created on first use): the readback's copy stream, the force pass's
-    // per-part chunk counters (device) and part flags (mapped host memory), the call counter
-    cudaStream_t copy_stream = nullptr;
-    uint32_t* part_done = nullptr;
-    uint32_t* part_flag = nullptr;
-    uint32_t* part_flag_dev = nullptr;
-    uint32_t readback_seq = 0;
+    HostReadback readback{};  // wc_fluid_update_host
     // L2 flush for timing
     float4* flush_buf = nullptr;
     size_t flush_n4 = 0;
@@ -82,9 +72,7 @@ void free_all(wc_fluid* f) {
     if (f->h_err) cudaFreeHost(f->h_err);
     if (f->exec) cudaGraphExecDestroy(f->exec);
     if (f->graph) cudaGraphDestroy(f->graph);
-    if (f->part_done) cudaFree(f->part_done);
-    if (f->part_flag) cudaFreeHost(f->part_flag);
-    if (f->copy_stream) cudaStreamDestroy(f->copy_stream);
+    f->readback.release();
     if (f->stream) cudaStreamDestroy(f->stream);
 }
 
@@ -275,6 +263,52 @@ __global__ void iota_kernel(uint32_t* __restrict__ out, uint32_t n) {
 }  // namespace
 
 namespace wc {
+
+wc_status HostReadback::arm(cudaStream_t s, uint32_t n, float4* staging, StepInputs& step) {
+    if (!copy_stream) WC_CUDA_TRY(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+    if (!part_done) {
+        WC_TRY(dalloc(&part_done, READBACK_PARTS));
+        WC_CUDA_TRY(cudaMemsetAsync(part_done, 0, sizeof(uint32_t) * READBACK_PARTS, s));
+    }
+    if (!part_flag) {
+        WC_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&part_flag), sizeof(uint32_t) * READBACK_PARTS,
+                                  cudaHostAllocMapped));
+        std::memset(part_flag, 0, sizeof(uint32_t) * READBACK_PARTS);
+        WC_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&part_flag_dev), part_flag, 0));
+    }
+    if (++seq == 0) ++seq;  // the flags start at 0: no launch publishes 0
+    const uint32_t chunks = (n + 31u) >> 5;
+    part_chunks = (chunks + READBACK_PARTS - 1) / READBACK_PARTS;
+    parts = (chunks + part_chunks - 1) / part_chunks;
+    step.aos_out = staging;  // the pass writes the host records itself: no conversion kernel
+    step.part_done = part_done;
+    step.part_flag = part_flag_dev;
+    step.part_chunks = part_chunks;
+    step.seq = seq;
+    return WC_OK;
+}
+
+wc_status HostReadback::drain(cudaStream_t s, uint32_t n, const float4* staging, wc_particle* out) {
+    const volatile uint32_t* flag = part_flag;
+    for (uint32_t r = 0; r < parts; ++r) {
+        // part r is published once its last chunk is stored; a stream that has ended (or failed)
+        // without the flag ends the wait too, and the copy then reads what the stream left
+        for (uint32_t spin = 1; flag[r] != seq; ++spin)
+            if ((spin & 1023u) == 0u && cudaStreamQuery(s) != cudaErrorNotReady) break;
+        const uint32_t s0 = r * part_chunks * 32u, s1 = std::min((r + 1) * part_chunks * 32u, n);
+        WC_CUDA_TRY(cudaMemcpyAsync(out + s0, staging + 2 * (size_t)s0, sizeof(wc_particle) * (size_t)(s1 - s0),
+                                    cudaMemcpyDeviceToHost, copy_stream));
+    }
+    WC_CUDA_TRY(cudaStreamSynchronize(copy_stream));
+    return WC_OK;
+}
+
+void HostReadback::release() {
+    if (part_done) cudaFree(part_done);
+    if (part_flag) cudaFreeHost(part_flag);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    *this = HostReadback{};
+}
 
 FluidInternals fluid_internals(wc_fluid* f) {
     return FluidInternals{&f->d, &f->sc, &f->in, &f->params, f->stream};
@@ -476,44 +510,14 @@ WC_API wc_status wc_fluid_update_host(wc_fluid* f, double time, const wc_particl
     f->in.dt = (float)time * f->params.time_scale;  // Fluid.cpp:308
     if (in) WC_TRY(enqueue_upload(f, true, in, n));  // the final wait covers the copy from in
     WC_TRY(ensure_staging(f));
-    if (!f->copy_stream) WC_CUDA_TRY(cudaStreamCreateWithFlags(&f->copy_stream, cudaStreamNonBlocking));
-    if (!f->part_done) {
-        WC_TRY(dalloc(&f->part_done, READBACK_PARTS));
-        WC_CUDA_TRY(cudaMemsetAsync(f->part_done, 0, sizeof(uint32_t) * READBACK_PARTS, f->stream));
-    }
-    if (!f->part_flag) {
-        WC_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&f->part_flag), sizeof(uint32_t) * READBACK_PARTS,
-                                  cudaHostAllocMapped));
-        std::memset(f->part_flag, 0, sizeof(uint32_t) * READBACK_PARTS);
-        WC_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&f->part_flag_dev), f->part_flag, 0));
-    }
-    if (++f->readback_seq == 0) ++f->readback_seq;  // flags start at 0: never publish 0
-    const uint32_t seq = f->readback_seq;
-    const uint32_t chunks = (n + 31u) >> 5;
-    const uint32_t part_chunks = (chunks + READBACK_PARTS - 1) / READBACK_PARTS;
-    const uint32_t parts = (chunks + part_chunks - 1) / part_chunks;
     StepInputs step = f->in;
-    step.aos_out = f->staging;  // the pass writes the host records itself: no conversion kernel
-    step.part_done = f->part_done;
-    step.part_flag = f->part_flag_dev;
-    step.part_chunks = part_chunks;
-    step.seq = seq;
+    WC_TRY(f->readback.arm(f->stream, n, f->staging, step));
     // the step of the graph, launched directly with the readback fields
     enqueue_sort(f);
     launch_density(f->d, f->sc, f->ld, f->stream);
     launch_force(f->d, f->sc, step, f->ld, f->stream);
     WC_TRY(check_launch());
-    const volatile uint32_t* flag = f->part_flag;
-    for (uint32_t r = 0; r < parts; ++r) {
-        // part r is published once its last chunk is stored; a stream that has ended (or failed)
-        // without the flag ends the wait too, and the copy then reads what the stream left
-        for (uint32_t spin = 1; flag[r] != seq; ++spin)
-            if ((spin & 1023u) == 0u && cudaStreamQuery(f->stream) != cudaErrorNotReady) break;
-        const uint32_t s0 = r * part_chunks * 32u, s1 = std::min((r + 1) * part_chunks * 32u, n);
-        WC_CUDA_TRY(cudaMemcpyAsync(out + s0, f->staging + 2 * (size_t)s0, sizeof(wc_particle) * (size_t)(s1 - s0),
-                                    cudaMemcpyDeviceToHost, f->copy_stream));
-    }
-    WC_CUDA_TRY(cudaStreamSynchronize(f->copy_stream));
+    WC_TRY(f->readback.drain(f->stream, n, f->staging, out));
     ++f->steps;
     return read_device_errors(f);
 }

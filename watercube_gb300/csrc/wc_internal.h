@@ -232,6 +232,28 @@ void launch_aos_to_soa(const float4* aos, float4* pos, float4* vel, uint32_t n, 
 void launch_soa_to_aos(const float4* pos, const float4* vel, float4* aos, uint32_t n, cudaStream_t s);
 void launch_l2_flush(const float4* buf, size_t n4, float* sink, cudaStream_t s);
 
+// A readback that overlaps the lane force pass (wc_fluid_update_host, wc_batch_step_host): the
+// state's slots form READBACK_PARTS parts of whole chunks; the pass writes each stored particle's
+// host record into the staging buffer and flags each finished part in mapped host memory
+// (StepInputs readback fields); the host polls the flags in order and copies each part out on a
+// second stream as it appears, so only the last part's copy follows the pass. No GPU-side wait.
+constexpr uint32_t READBACK_PARTS = 8;
+struct HostReadback {
+    cudaStream_t copy_stream = nullptr;
+    uint32_t* part_done = nullptr;      // device: finished chunks per part, zero between launches
+    uint32_t* part_flag = nullptr;      // mapped host memory: the sequence number of the last
+    uint32_t* part_flag_dev = nullptr;  // launch that finished each part, and its device address
+    uint32_t seq = 0;
+    uint32_t part_chunks = 0;
+    uint32_t parts = 0;
+    // Creates what is missing (on `s`) and sets the readback fields of `step` for n slots.
+    wc_status arm(cudaStream_t s, uint32_t n, float4* staging, StepInputs& step);
+    // After the pass is enqueued on `s`: copies the parts into out as they are flagged (or once
+    // `s` has ended), then waits for the copies.
+    wc_status drain(cudaStream_t s, uint32_t n, const float4* staging, wc_particle* out);
+    void release();
+};
+
 // The same stages over a batch of scenes (wc_batch.cu): keys carry the scene's cell offset and
 // every cell takes its scene's constants.
 void launch_bin_count_batched(const DevBuffers& d, const BatchTables& bt, const LaunchDims& ld, cudaStream_t s);
