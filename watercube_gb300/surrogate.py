@@ -311,3 +311,42 @@ class Trainer:
         for f in self._fluids.values():
             f.close()
         self._fluids.clear()
+
+
+def main(argv=None) -> dict:
+    """`python -m watercube_gb300.surrogate`: a judged rollout of the message-passing surrogate on
+    the dam break from its initial state (the trained weights when present), printing the rollout
+    statistics as one JSON line."""
+    import argparse
+    import json
+
+    from .fluid import dam_break_params, finalize, generate_dam_break
+    from .train_surrogate import DEFAULT_WEIGHTS, load_weights
+
+    modes = {"sph": WC_ROLLOUT_SPH, "surrogate": WC_ROLLOUT_SURROGATE, "stale": WC_ROLLOUT_STALE,
+             "hybrid": WC_ROLLOUT_HYBRID}
+    ap = argparse.ArgumentParser(description="Judged rollout of the message-passing surrogate on the dam break "
+                                             "(prints the rollout statistics as one JSON line)")
+    ap.add_argument("--particles", type=int, default=1048576)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--K", type=int, default=4, help="a plain SPH judge step every K steps")
+    ap.add_argument("--dt", type=float, default=2.5e-4)
+    ap.add_argument("--mode", choices=sorted(modes), default="surrogate")
+    args = ap.parse_args(argv)
+    check(lib().wc_set_device(0), "wc_set_device")
+    p = finalize(dam_break_params(args.particles))
+    st = generate_dam_break(p, 0)
+    s = load_weights() if DEFAULT_WEIGHTS.is_file() else Surrogate(layers=8, seed=1)
+    try:
+        with Fluid.create("rollout", p) as f:
+            f.setup(st)
+            r = rollout(f, args.dt, args.steps, args.K, 0.01, modes[args.mode], s)
+    finally:
+        s.close()
+    r.update(particles=args.particles, mode=args.mode, K=args.K)
+    print(json.dumps(r), flush=True)
+    return r
+
+
+if __name__ == "__main__":
+    main()
