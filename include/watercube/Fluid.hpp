@@ -123,6 +123,12 @@ public:
     }
     // One step of dt = float(time) * time scale, enqueued on the fluid's stream.
     void update(double time) { check(wc_fluid_update(require(), time), "update"); }
+    // update(time) with host buffers (wc_fluid_update_host): uploads `in` first when it is not
+    // null, and returns with the stepped state in `out` (num_particles entries), read back while
+    // the step's force pass runs.
+    void updateHost(double time, const wc_particle* in, wc_particle* out) {
+        check(wc_fluid_update_host(require(), time, in, out, params_.num_particles), "updateHost");
+    }
     void draw() {}
     void reset() {}
 

@@ -3,6 +3,7 @@
 // Prints "ok <particles> <steps>" and exits 0 when every particle stays finite inside the box.
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 
 #include "watercube/Fluid.hpp"
 
@@ -15,6 +16,16 @@ int main() {
         for (int i = 0; i < frames; ++i) fluid->update(1.0 / 60.0);
         const std::vector<wc_particle> p = fluid->particles();
         const std::vector<uint32_t> counts = fluid->uints(WC_UINTS_CELL_COUNTS);
+        // one frame with host buffers equals upload + update + readback
+        std::vector<wc_particle> stepped(p.size());
+        fluid->updateHost(1.0 / 60.0, p.data(), stepped.data());
+        if (fluid->particles().size() != stepped.size()) return 1;
+        const std::vector<wc_particle> again = fluid->particles();
+        for (size_t i = 0; i < again.size(); ++i)
+            if (std::memcmp(&again[i], &stepped[i], sizeof(wc_particle)) != 0) {
+                std::printf("updateHost readback differs from particles() at %zu\n", i);
+                return 1;
+            }
         fluid->synchronize();
         uint64_t total = 0;
         for (uint32_t c : counts) total += c;
