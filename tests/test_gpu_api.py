@@ -7,7 +7,7 @@ import pytest
 
 from helpers import case, fluid
 from watercube_gb300 import _abi
-from watercube_gb300.fluid import Fluid
+from watercube_gb300.fluid import Fluid, finalize
 
 pytestmark = pytest.mark.gpu
 
@@ -122,6 +122,27 @@ def test_update_host_equals_the_three_calls(gpu, flags, pinned):
         finally:
             for buf in bufs:
                 buf.free()
+
+
+@pytest.mark.parametrize("n", [1, 45, 1000, 12345])
+def test_update_host_ragged_sizes(gpu, n):
+    """Particle counts that leave a partial last chunk of 32 slots and parts of one chunk or a few
+    (the readback's part bookkeeping): the same bytes as set_particles + update + particles()."""
+    from watercube_gb300.fluid import generate_reference_lattice, reference_params
+
+    p = reference_params()
+    p.num_particles = n
+    p = finalize(p)
+    st = generate_reference_lattice(p, 0)
+    with fluid(p, st) as a, fluid(p, st) as b:
+        cur = st.copy()
+        out = np.empty_like(st)
+        for _ in range(3):
+            a.update_host(1.0 / 60.0, cur, out)
+            b.set_particles(cur)
+            b.update(1.0 / 60.0)
+            assert out.tobytes() == b.particles().tobytes(), n
+            cur = out.copy()
 
 
 def test_update_host_checks_its_arguments(gpu):
