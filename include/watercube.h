@@ -446,6 +446,13 @@ typedef struct wc_gemm_desc {
     uint32_t ldc;
     size_t split_stride;
     int accumulate;        /* non-zero: c_f32 += result */
+    /* LayerNorm epilogue when ln_gamma is set (n = 128, plain row-major A and B^T, BF16 output
+       only, no ReLU, gathers or accumulation): c_bf16 = LN(A . B (+ bias)) * ln_gamma + ln_beta
+       (+ ln_resid, BF16 rows of 128), the row's mean and variance over its 128 columns in FP32,
+       epsilon 1e-5 */
+    const float* ln_gamma;
+    const float* ln_beta;
+    const void* ln_resid;  /* bf16, or NULL */
 } wc_gemm_desc;
 
 WC_API wc_status wc_nn_gemm(const wc_gemm_desc* g, uint32_t* d_err, void* stream);

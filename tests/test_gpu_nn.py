@@ -119,3 +119,38 @@ def test_persistent_pipeline_many_tiles(wclib, torch, m, n, k):
     ref = torch.relu(a.float() @ wt.float().t() + bias)
     close(c, ref)
     close(c16, ref, rel=1e-3 + 2.0 ** -8)
+
+
+@pytest.mark.parametrize("m,k,bias,resid", [(300, 128, True, True), (77, 256, False, True), (20000, 128, True, False),
+                                             (58445, 384, True, True)])
+def test_layernorm_epilogue(wclib, torch, m, k, bias, resid):
+    """C = LN(A . W^T (+ b)) * gamma + beta (+ resid) in the GEMM's epilogue (the message-passing
+    rollout's fused second MLP layers) against the same in FP32 on the BF16 inputs: the row
+    statistics in FP32 (a different summation order), then one BF16 rounding of the output."""
+    n = 128
+    a = rnd(torch, m, k, seed=21)
+    wt = rnd(torch, n, k, seed=22)
+    b = torch.randn(n, device="cuda") if bias else None
+    gamma = torch.rand(n, device="cuda") + 0.5
+    beta = torch.randn(n, device="cuda") * 0.1
+    r = rnd(torch, m, n, seed=23) if resid else None
+    c = torch.zeros(m, n, device="cuda", dtype=torch.bfloat16)
+    kw = dict(m=m, n=n, k=k, a=a, lda=k, b=wt, ldb=k, c_bf16=c, ldc=n, ln_gamma=gamma, ln_beta=beta)
+    if bias:
+        kw["bias"] = b
+    if resid:
+        kw["ln_resid"] = r
+    run(wclib, torch, **kw)
+    y = a.float() @ wt.float().t() + (b if bias else 0.0)
+    ref = torch.nn.functional.layer_norm(y, (n,), gamma, beta, eps=1e-5) + (r.float() if resid else 0.0)
+    close(c, ref, rel=8e-3)
+
+
+def test_layernorm_epilogue_rejects_other_forms(wclib, torch):
+    a = rnd(torch, 64, 64, seed=1)
+    wt = rnd(torch, 96, 64, seed=2)
+    gamma = torch.ones(96, device="cuda")
+    c = torch.zeros(64, 96, device="cuda", dtype=torch.bfloat16)
+    g = _abi.GemmDesc(m=64, n=96, k=64, k_chunk=64, a=a.data_ptr(), lda=64, b=wt.data_ptr(), ldb=64,
+                      c_bf16=c.data_ptr(), ldc=96, ln_gamma=gamma.data_ptr(), ln_beta=gamma.data_ptr())
+    assert wclib.wc_nn_gemm(C.byref(g), None, None) == _abi.WC_ERR_INVALID_ARG  # n must be 128

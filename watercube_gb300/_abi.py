@@ -163,7 +163,7 @@ class GemmDesc(C.Structure):
         ("bias", C.c_void_p), ("add1", C.c_void_p), ("add1_idx", C.c_void_p), ("add2", C.c_void_p),
         ("add2_idx", C.c_void_p), ("ld_add", C.c_uint32), ("relu", C.c_int),
         ("c_f32", C.c_void_p), ("c_bf16", C.c_void_p), ("ldc", C.c_uint32), ("split_stride", C.c_size_t),
-        ("accumulate", C.c_int),
+        ("accumulate", C.c_int), ("ln_gamma", C.c_void_p), ("ln_beta", C.c_void_p), ("ln_resid", C.c_void_p),
     ]
 
 

@@ -34,9 +34,15 @@ struct GemmArgs {
     __nv_bfloat16* c_bf16;
     uint32_t ldc;
     size_t split_stride;
+    // LayerNorm epilogue (ln_gamma set): c_bf16 = LN(result) * ln_gamma + ln_beta (+ ln_resid rows)
+    const float* ln_gamma;
+    const float* ln_beta;
+    const __nv_bfloat16* ln_resid;
 };
 
 size_t gemm_smem_bytes();
+// Whether launch_gemm can run a LayerNorm-epilogue GEMM (the TMA kernel's tensor maps exist).
+bool gemm_ln_available();
 wc_status check_gemm(const GemmArgs& g);
 wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s);
 

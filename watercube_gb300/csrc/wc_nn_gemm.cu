@@ -497,6 +497,146 @@ __device__ __forceinline__ void drain_accumulators(const GemmArgs& g, uint32_t t
     }
 }
 
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t v[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+
+// The LayerNorm epilogue (GemmArgs::ln_gamma, n = 128, one column of tiles): the two warps that
+// read the same 32 accumulator lanes (`quarter`) hold a row's 128 columns between them, 64 each
+// (`half`). Each thread sums its 64 values, the pair exchanges the sums through shared memory at
+// a named barrier of its 64 threads (ids 1 .. 4), then the squared deviations from the mean the
+// same way, and each thread normalises, scales and shifts its own columns, adds the residual row
+// and stores BF16. Both warps of a pair pass both barriers of every tile: whether each warp's
+// accumulator wait succeeded is exchanged at the first barrier and the pair leaves together.
+__device__ __forceinline__ void pair_sync(uint32_t quarter) {
+    asm volatile("bar.sync %0, 64;" ::"r"(1u + quarter) : "memory");
+}
+
+__device__ __forceinline__ void drain_accumulators_ln(const GemmArgs& g, uint32_t tmem, uint64_t* acc_full,
+                                                      uint64_t* acc_empty, volatile int* failed, uint32_t ntiles,
+                                                      uint32_t nslices, uint32_t quarter, uint32_t half,
+                                                      uint32_t lane, float (*xs)[2][32], float (*xv)[2][32],
+                                                      int (*oks)[2]) {
+    constexpr float LN_EPSILON = 1e-5f;
+    const uint32_t col0 = 64u * half;
+    // bias, gamma and beta four at a time when all three allow 16-byte loads (uniform branch)
+    const bool vec = ((reinterpret_cast<uintptr_t>(g.ln_gamma) | reinterpret_cast<uintptr_t>(g.ln_beta) |
+                       reinterpret_cast<uintptr_t>(g.bias)) & 15u) == 0;
+    uint32_t t = 0;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
+        const uint32_t b = t & 1u;
+        bool ok = !*failed && mbar_wait(smem_addr(&acc_full[b]), (t >> 1) & 1u);
+        ok = __all_sync(0xffffffffu, ok);
+        float x[64];
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t taddr = tmem + ((32u * quarter) << 16) + b * (uint32_t)BN + col0;
+            uint32_t v[32];
+            tmem_ld32(taddr, v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 32; ++j) x[j] = nslices ? __uint_as_float(v[j]) : 0.f;
+            tmem_ld32(taddr + 32u, v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 32; ++j) x[32 + j] = nslices ? __uint_as_float(v[j]) : 0.f;
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 64; ++j) x[j] = 0.f;
+        }
+        if (g.bias) {
+            if (vec) {
+#pragma unroll
+                for (int j = 0; j < 64; j += 4) {
+                    const float4 bb = __ldg(reinterpret_cast<const float4*>(g.bias + col0 + j));
+                    x[j] += bb.x;
+                    x[j + 1] += bb.y;
+                    x[j + 2] += bb.z;
+                    x[j + 3] += bb.w;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 64; ++j) x[j] += __ldg(g.bias + col0 + j);
+            }
+        }
+        float sum = 0.f;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) sum += x[j];
+        xs[quarter][half][lane] = sum;
+        if (lane == 0) oks[quarter][half] = ok ? 1 : 0;
+        pair_sync(quarter);
+        if (!(oks[quarter][0] && oks[quarter][1])) {
+            if (lane == 0) *failed = 1;
+            break;
+        }
+        const float mean = (xs[quarter][0][lane] + xs[quarter][1][lane]) * (1.f / 128.f);
+        float sq = 0.f;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+            x[j] -= mean;
+            sq += x[j] * x[j];
+        }
+        xv[quarter][half][lane] = sq;
+        pair_sync(quarter);
+        const float var = (xv[quarter][0][lane] + xv[quarter][1][lane]) * (1.f / 128.f);
+        const float rstd = rsqrtf(var + LN_EPSILON);
+        const uint32_t row = tile * BM + 32u * quarter + lane;
+        if (row >= g.m) continue;
+        const __nv_bfloat16* res = g.ln_resid ? g.ln_resid + (size_t)row * 128u + col0 : nullptr;
+        __nv_bfloat16* out = g.c_bf16 + (size_t)row * g.ldc + col0;
+#pragma unroll
+        for (int c = 0; c < 64; c += 8) {
+            float gm[8], bt[8];
+            if (vec) {
+#pragma unroll
+                for (int k = 0; k < 8; k += 4) {
+                    const float4 g4 = __ldg(reinterpret_cast<const float4*>(g.ln_gamma + col0 + c + k));
+                    const float4 b4 = __ldg(reinterpret_cast<const float4*>(g.ln_beta + col0 + c + k));
+                    gm[k] = g4.x, gm[k + 1] = g4.y, gm[k + 2] = g4.z, gm[k + 3] = g4.w;
+                    bt[k] = b4.x, bt[k + 1] = b4.y, bt[k + 2] = b4.z, bt[k + 3] = b4.w;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    gm[k] = __ldg(g.ln_gamma + col0 + c + k);
+                    bt[k] = __ldg(g.ln_beta + col0 + c + k);
+                }
+            }
+            float o[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) o[k] = x[c + k] * rstd * gm[k] + bt[k];
+            if (res) {
+                const uint4 rv = __ldg(reinterpret_cast<const uint4*>(res + c));
+                const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&rv);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float2 f = __bfloat1622float2(h[k]);
+                    o[2 * k] += f.x;
+                    o[2 * k + 1] += f.y;
+                }
+            }
+            uint4 w;
+            __nv_bfloat162 q0 = __floats2bfloat162_rn(o[0], o[1]), q1 = __floats2bfloat162_rn(o[2], o[3]);
+            __nv_bfloat162 q2 = __floats2bfloat162_rn(o[4], o[5]), q3 = __floats2bfloat162_rn(o[6], o[7]);
+            w.x = *reinterpret_cast<uint32_t*>(&q0);
+            w.y = *reinterpret_cast<uint32_t*>(&q1);
+            w.z = *reinterpret_cast<uint32_t*>(&q2);
+            w.w = *reinterpret_cast<uint32_t*>(&q3);
+            *reinterpret_cast<uint4*>(out + c) = w;
+        }
+    }
+}
+
 template <bool RB>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) gemm_pipe_kernel(const GemmArgs g, uint32_t* err) {
     constexpr int STAGES = PipeShape<RB>::STAGES, LAG = PipeShape<RB>::LAG;
@@ -681,12 +821,16 @@ __device__ __forceinline__ void tma_load_box(const CUtensorMap* map, void* dst, 
         : "memory");
 }
 
+template <bool LN>
 __global__ void __launch_bounds__(TMA_THREADS, 1) gemm_tma_kernel(const GemmArgs g,
                                                                   const __grid_constant__ CUtensorMap map_a,
                                                                   const __grid_constant__ CUtensorMap map_b,
                                                                   uint32_t* err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ uint64_t full[TMA_STAGES], empty[TMA_STAGES], acc_full[2], acc_empty[2], b_full;
+    // LN: the warp pairs' exchanged row sums, squared deviations and wait outcomes
+    __shared__ float s_lnx[LN ? 4 : 1][2][32], s_lnv[LN ? 4 : 1][2][32];
+    __shared__ int s_lnok[LN ? 4 : 1][2];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_failed;
     volatile int* failed = &s_failed;
@@ -786,8 +930,12 @@ __global__ void __launch_bounds__(TMA_THREADS, 1) gemm_tma_kernel(const GemmArgs
         __syncwarp();
     } else {
         // warps 2..9: quarter w % 4, columns 64 ((w - 2) / 4) ..
-        drain_accumulators(g, tmem, acc_full, acc_empty, failed, ntiles, tiles_n, nslices, warp & 3u, (warp - 2u) / 4u,
-                           lane);
+        if constexpr (LN)
+            drain_accumulators_ln(g, tmem, acc_full, acc_empty, failed, ntiles, nslices, warp & 3u, (warp - 2u) / 4u,
+                                  lane, s_lnx, s_lnv, s_lnok);
+        else
+            drain_accumulators(g, tmem, acc_full, acc_empty, failed, ntiles, tiles_n, nslices, warp & 3u,
+                               (warp - 2u) / 4u, lane);
     }
     __syncthreads();
     if (*failed && threadIdx.x == 0 && err) atomicOr(err, DEVERR_MMA_TIMEOUT);
@@ -816,6 +964,11 @@ wc_status check_gemm(const GemmArgs& g) {
         return fail(WC_ERR_INVALID_ARG, "gemm: k must be a multiple of 8 (pad with zeros)");
     if ((g.add1 && !g.add1_idx) || (g.add2 && !g.add2_idx)) return fail(WC_ERR_INVALID_ARG, "gemm: gather without index");
     if (g.k_chunk == 0 || g.k_chunk % BK) return fail(WC_ERR_INVALID_ARG, "gemm: k_chunk must be a multiple of 64");
+    if (g.ln_gamma && (g.n != 128u || !g.ln_beta || !g.c_bf16 || g.c_f32 || g.relu || g.add1 || g.add2 ||
+                       g.accumulate || g.ldc != 128u || g.a_rows || g.a2 || g.a_transposed || g.b_rowmajor ||
+                       g.k_chunk < g.k))
+        return fail(WC_ERR_INVALID_ARG,
+                    "gemm: the LayerNorm epilogue needs n = ldc = 128, beta, a BF16 output only and plain operands");
     return WC_OK;
 }
 
@@ -857,6 +1010,8 @@ bool encode_operand(CUtensorMap* map, const void* base, uint64_t inner, uint64_t
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool gemm_ln_available() { return encode_tiled() != nullptr; }
+
 wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s) {
     const wc_status st = check_gemm(g);
     if (st != WC_OK || g.m == 0 || g.n == 0) return st;
@@ -883,16 +1038,22 @@ wc_status launch_gemm(const GemmArgs& g, uint32_t* err, cudaStream_t s) {
             if (encode_operand(&ma, g.a, g.k, g.m, 2ull * g.lda) && encode_operand(&mb, g.b, g.k, g.n, 2ull * g.ldb)) {
                 static bool tma_attr = false;
                 if (!tma_attr) {
-                    cudaFuncSetAttribute(gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    cudaFuncSetAttribute(gemm_tma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)pipe_smem_bytes(true, RB_MAX_SLICES * BK));
+                    cudaFuncSetAttribute(gemm_tma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)pipe_smem_bytes(true, RB_MAX_SLICES * BK));
                     tma_attr = true;
                 }
-                gemm_tma_kernel<<<grid, TMA_THREADS, pipe_smem_bytes(true, g.k), s>>>(g, ma, mb, err);
+                if (g.ln_gamma)
+                    gemm_tma_kernel<true><<<grid, TMA_THREADS, pipe_smem_bytes(true, g.k), s>>>(g, ma, mb, err);
+                else
+                    gemm_tma_kernel<false><<<grid, TMA_THREADS, pipe_smem_bytes(true, g.k), s>>>(g, ma, mb, err);
                 const cudaError_t e = cudaGetLastError();
                 if (e != cudaSuccess) return fail(WC_ERR_CUDA, "gemm launch: %s", cudaGetErrorString(e));
                 return WC_OK;
             }
         }
+        if (g.ln_gamma) return fail(WC_ERR_STATE, "gemm: the LayerNorm epilogue needs the TMA kernel (plain A, k <= 384)");
         if (rb)
             gemm_pipe_kernel<true><<<grid, PIPE_THREADS, pipe_smem_bytes(true, g.k), s>>>(g, err);
         else
@@ -946,5 +1107,8 @@ extern "C" WC_API wc_status wc_nn_gemm(const wc_gemm_desc* d, uint32_t* d_err, v
     g.c_bf16 = static_cast<__nv_bfloat16*>(d->c_bf16);
     g.ldc = d->ldc;
     g.split_stride = d->split_stride;
+    g.ln_gamma = d->ln_gamma;
+    g.ln_beta = d->ln_beta;
+    g.ln_resid = static_cast<const __nv_bfloat16*>(d->ln_resid);
     return wc::nn::launch_gemm(g, d_err, static_cast<cudaStream_t>(stream));
 }

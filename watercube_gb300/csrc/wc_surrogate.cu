@@ -242,6 +242,28 @@ wc_status fwd(wc_surrogate* s, const Lin& l, uint32_t rows, const __nv_bfloat16*
     return launch_gemm(g, s->d_err, s->stream);
 }
 
+// out = LN(a . W^T + b) * gamma + beta (+ resid) in one GEMM with the LayerNorm in its epilogue
+// (the forward pass of a rollout, which keeps no activations for a backward pass).
+wc_status fwd_ln(wc_surrogate* s, const Lin& l, uint32_t rows, const __nv_bfloat16* a, const float* gamma,
+                 const __nv_bfloat16* resid, __nv_bfloat16* out) {
+    GemmArgs g{};
+    g.m = rows;
+    g.n = l.nout;
+    g.k = l.kin;
+    g.k_chunk = ((l.kin + 63) / 64) * 64;
+    g.a = a;
+    g.lda = l.kin;
+    g.b = s->wb + l.wt;
+    g.ldb = l.kin;
+    g.bias = l.b != NONE ? s->w + l.b : nullptr;
+    g.c_bf16 = out;
+    g.ldc = l.nout;
+    g.ln_gamma = gamma;
+    g.ln_beta = gamma + W;
+    g.ln_resid = resid;
+    return launch_gemm(g, s->d_err, s->stream);
+}
+
 // dX (rows x kcount) (+)= dY . W[k0 : k0 + kcount]^T
 wc_status dgrad(wc_surrogate* s, const Lin& l, uint32_t rows, const __nv_bfloat16* dy, uint32_t k0, uint32_t kcount,
                 float* dx, bool accumulate) {
@@ -472,17 +494,29 @@ wc_status prepare_sample(wc_surrogate* s, wc_fluid* f, bool saved, const float4*
 
 // ---- forward / backward ---------------------------------------------------------------------
 
-wc_status forward(wc_surrogate* s) {
+// keep: the activations and LayerNorm statistics the backward pass reads (training); without
+// it every second MLP layer and its LayerNorm run as one GEMM with the LayerNorm in the epilogue.
+wc_status forward(wc_surrogate* s, bool keep) {
     if (s->cast_dirty) cast_all(s);
     Work& w = s->work;
     const uint32_t n = s->n, e = s->e;
+    const bool fuse = !keep && gemm_ln_available();
     float* st = w.stn0;
     WC_TRY(fwd(s, s->ne1, n, w.xn, nullptr, true, nullptr, w.zn0));
-    WC_TRY(fwd(s, s->ne2, n, w.zn0, nullptr, false, w.yn0, nullptr));
-    layernorm(n, w.yn0, s->w + s->lnn0.g, s->w + s->lnn0.g + W, nullptr, hbuf(w, 0), st, st + n, s->stream);
+    if (fuse) {
+        WC_TRY(fwd_ln(s, s->ne2, n, w.zn0, s->w + s->lnn0.g, nullptr, hbuf(w, 0)));
+    } else {
+        WC_TRY(fwd(s, s->ne2, n, w.zn0, nullptr, false, w.yn0, nullptr));
+        layernorm(n, w.yn0, s->w + s->lnn0.g, s->w + s->lnn0.g + W, nullptr, hbuf(w, 0), st, st + n, s->stream);
+    }
     WC_TRY(fwd(s, s->ee1, e, w.xe, nullptr, true, nullptr, w.ze0));
-    WC_TRY(fwd(s, s->ee2, e, w.ze0, nullptr, false, w.ye0, nullptr));
-    layernorm(e, w.ye0, s->w + s->lne0.g, s->w + s->lne0.g + W, nullptr, ebuf(w, 0), w.ste0, w.ste0 + e, s->stream);
+    if (fuse) {
+        WC_TRY(fwd_ln(s, s->ee2, e, w.ze0, s->w + s->lne0.g, nullptr, ebuf(w, 0)));
+    } else {
+        WC_TRY(fwd(s, s->ee2, e, w.ze0, nullptr, false, w.ye0, nullptr));
+        layernorm(e, w.ye0, s->w + s->lne0.g, s->w + s->lne0.g + W, nullptr, ebuf(w, 0), w.ste0, w.ste0 + e,
+                  s->stream);
+    }
     const size_t pn = (size_t)w.cap_n * W, pe = (size_t)w.cap_e * W;
     for (uint32_t l = 0; l < s->L; ++l) {
         const MPLayer& L = s->layers[l];
@@ -497,12 +531,20 @@ wc_status forward(wc_surrogate* s) {
         WC_TRY(fwd(s, L.e1i, n, h, nullptr, false, nullptr, w.P));
         WC_TRY(fwd(s, L.e1s, n, h, nullptr, false, nullptr, w.Q));
         WC_TRY(fwd(s, L.e1e, e, el, nullptr, true, nullptr, ze, w.P, w.recv, w.Q, w.col));
-        WC_TRY(fwd(s, L.e2, e, ze, nullptr, false, ye, nullptr));
-        layernorm(e, ye, s->w + L.lne.g, s->w + L.lne.g + W, el, e1, ste, ste + e, s->stream);
+        if (fuse) {
+            WC_TRY(fwd_ln(s, L.e2, e, ze, s->w + L.lne.g, el, e1));
+        } else {
+            WC_TRY(fwd(s, L.e2, e, ze, nullptr, false, ye, nullptr));
+            layernorm(e, ye, s->w + L.lne.g, s->w + L.lne.g + W, el, e1, ste, ste + e, s->stream);
+        }
         segment_sum_bf16(n, w.rowptr, nullptr, e1, nullptr, agg, s->stream);
         WC_TRY(fwd(s, L.n1, n, h, agg, true, nullptr, zn));
-        WC_TRY(fwd(s, L.n2, n, zn, nullptr, false, yn, nullptr));
-        layernorm(n, yn, s->w + L.lnn.g, s->w + L.lnn.g + W, h, h1, stn, stn + n, s->stream);
+        if (fuse) {
+            WC_TRY(fwd_ln(s, L.n2, n, zn, s->w + L.lnn.g, h, h1));
+        } else {
+            WC_TRY(fwd(s, L.n2, n, zn, nullptr, false, yn, nullptr));
+            layernorm(n, yn, s->w + L.lnn.g, s->w + L.lnn.g + W, h, h1, stn, stn + n, s->stream);
+        }
     }
     WC_TRY(fwd(s, s->d1, n, hbuf(w, s->L), nullptr, true, nullptr, w.zd));
     WC_TRY(fwd(s, s->d2, n, w.zd, nullptr, false, w.out, nullptr));
@@ -698,14 +740,14 @@ struct RolloutRun {
                 // in a rollout: the stale input is already sorted)
                 gather4(D.n, D.perm, s->stale, s->stale_tmp, fi.stream);
                 WC_TRY(prepare_sample(s, f, false, s->stale_tmp, true, age));
-                WC_TRY(forward(s));
+                WC_TRY(forward(s, false));
                 add_scaled(D.n, s->work.out, OUT, s->cfg.accel_scale, s->stale_tmp, s->work.stale_s, fi.stream);
                 acc = reinterpret_cast<const float*>(s->work.stale_s);
                 ld = 4;
                 scale = 1.0f;
             } else {
                 WC_TRY(prepare_sample(s, f, false));
-                WC_TRY(forward(s));
+                WC_TRY(forward(s, false));
                 acc = s->work.out;
                 ld = OUT;
                 scale = s->cfg.accel_scale;
@@ -997,7 +1039,7 @@ WC_API wc_status wc_surrogate_forward_backward(wc_surrogate* s, int do_backward,
     WC_NVTX("wc_surrogate_forward_backward");
     if (!s || !s->fluid) return fail(WC_ERR_STATE, "no sample loaded (wc_surrogate_sample)");
     if (do_backward && !s->has_target) return fail(WC_ERR_STATE, "backward needs a sample with targets");
-    WC_TRY(forward(s));
+    WC_TRY(forward(s, do_backward != 0));
     Work& w = s->work;
     if (s->has_target) {
         mse(s->n, OUT, w.out, w.target_s, 1.0f / s->cfg.accel_scale, do_backward ? w.dout : nullptr,
