@@ -21,7 +21,6 @@ const char* const STEP_KERNEL_NAMES[NUM_STEP_KERNELS] = {"bin_count", "scan_cell
 
 bool same_inputs(const StepInputs& a, const StepInputs& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
 
-
 }  // namespace
 
 struct wc_fluid {
