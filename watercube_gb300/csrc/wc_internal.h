@@ -134,8 +134,10 @@ constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;  // ~0.3-1 s of polling before gi
 constexpr int SPH_THREADS = 256;
 // Candidates a warp stages in shared memory per cell in the density pass (padding included).
 constexpr int STAGE_CAP = 320;
-// 32-bit words of neighbour bit strings per particle (density pass -> force pass).
-constexpr int MASK_WORDS = 48;
+// 32-bit words of neighbour bit strings per particle (density pass -> force pass): room for 4,096
+// candidates, the 27-cell neighbourhoods of the 1M dam break's most compressed states (99th
+// percentile 3,731 at step 1,750); a target with more tests its candidates again in the force pass.
+constexpr int MASK_WORDS = 128;
 // Force kernel dense path: per-lane neighbour list capacity ([CAP][32] words per warp).
 constexpr int FORCE_LIST_CAP = 16;
 
