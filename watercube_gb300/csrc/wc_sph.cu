@@ -882,25 +882,25 @@ __device__ __forceinline__ void pair_terms(const float4& pi, const float4& vi, c
 // A lane's list (entries list[e * 32 + lane], e < cnt), four entries per round so their loads
 // overlap; an empty place takes the particle itself (slot self), whose terms are exactly zero.
 // FEAT_FULL: also the neighbours' rates (rate[k]) and the target's pressure rate pdot_i.
-template <int FEAT>
+template <int FEAT, int ROUND = 4>
 __device__ __forceinline__ void accumulate_list(const uint32_t* list, uint32_t cnt, uint32_t lane, uint32_t self,
                                                 const float4& pi, const float4& vi, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vel, float h, float cull, float* f,
                                                 const float2* __restrict__ rate = nullptr, float pdot_i = 0.f) {
-    for (uint32_t e = 0; e < cnt; e += 4u) {
-        uint32_t k[4];
+    for (uint32_t e = 0; e < cnt; e += (uint32_t)ROUND) {
+        uint32_t k[ROUND];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) k[u] = e + (uint32_t)u < cnt ? list[(e + (uint32_t)u) * 32u + lane] : self;
-        float4 pj[4], vj[4];
-        float2 rj[4];
+        for (int u = 0; u < ROUND; ++u) k[u] = e + (uint32_t)u < cnt ? list[(e + (uint32_t)u) * 32u + lane] : self;
+        float4 pj[ROUND], vj[ROUND];
+        float2 rj[ROUND];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < ROUND; ++u) {
             pj[u] = __ldg(pos + k[u]);
             vj[u] = __ldg(vel + k[u]);
             rj[u] = FEAT == FEAT_FULL ? __ldg(rate + k[u]) : make_float2(0.f, 0.f);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], h, cull, f, pdot_i, rj[u]);
+        for (int u = 0; u < ROUND; ++u) pair_terms<FEAT>(pi, vi, pj[u], vj[u], h, cull, f, pdot_i, rj[u]);
     }
 }
 
@@ -1302,7 +1302,7 @@ __device__ __forceinline__ uint32_t slot_of(uint32_t q, const uint32_t P[9], con
 }
 
 template <bool BATCHED, int FEAT = FEAT_NONE>
-__global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 2 : 3) force_lane_kernel(
+__global__ void __launch_bounds__(SPH_THREADS, (FEAT == FEAT_FULL && BATCHED) ? 2 : 3) force_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const StepInputs in, const uint32_t n, const uint32_t num_cells,
     const float4* __restrict__ pos_b, const float4* __restrict__ vel_b, const uint32_t* __restrict__ ids_b,
     float4* __restrict__ pos_a, float4* __restrict__ vel_a, uint32_t* __restrict__ ids_a,
@@ -1401,7 +1401,10 @@ __global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 2 : 3) force_
                 }
             }
             if (!__any_sync(FULL, cnt > 0u)) break;
-            accumulate_list<FEAT>(list, cnt, lane, tself, pi, vi, pos_b, vel_b, sc.h, sc.cull, f, fb.rate, ri.y);
+            // J (FEAT_FULL) of a single scene: two neighbours per round, so that the pass fits 80
+            // registers and three blocks per SM (the batched one keeps four and two blocks)
+            accumulate_list<FEAT, (FEAT == FEAT_FULL && !BATCHED) ? 2 : 4>(list, cnt, lane, tself, pi, vi, pos_b, vel_b,
+                                                                          sc.h, sc.cull, f, fb.rate, ri.y);
             if (!__any_sync(FULL, more)) break;
         }
         if (live) {
