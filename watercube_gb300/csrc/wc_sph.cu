@@ -655,7 +655,7 @@ __device__ __forceinline__ uint32_t lane_rows(const uint32_t* __restrict__ tab, 
 }
 
 template <bool BATCHED, int FEAT = FEAT_NONE>
-__global__ void __launch_bounds__(SPH_THREADS, FEAT == FEAT_FULL ? 3 : 4) density_lane_kernel(
+__global__ void __launch_bounds__(SPH_THREADS, (FEAT == FEAT_FULL && BATCHED) ? 3 : 4) density_lane_kernel(
     const SceneConsts sc0, const BatchTables bt, const uint32_t n, const uint32_t num_cells,
     const float4* pos_in,  // its .w lanes are the density output: read with coherent loads
     float* rho_out, float* p_out, const uint32_t* __restrict__ start, const uint32_t* __restrict__ cell_list,
