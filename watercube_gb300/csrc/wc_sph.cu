@@ -1270,7 +1270,7 @@ __global__ void __launch_bounds__(SPH_THREADS, 4) force_kernel(const SceneConsts
 // round whenever it fills. Targets whose bit string was not kept (more than 32 MASK_WORDS
 // candidates) test their candidates directly.
 
-constexpr uint32_t LANE_LIST = 32;  // neighbour slots a lane collects before evaluating them
+constexpr uint32_t LANE_LIST = 48;  // neighbour slots a lane collects before evaluating them (48: 32 and 64 were slower)
 
 // Readback progress (StepInputs part fields): after chunk m every lane fences its stores, and the
 // warp that brings its part's count to the part's size publishes the part: the counter goes back
