@@ -129,6 +129,31 @@ def test_gradients_match_fp64_oracle(gpu, layers, n, age):
     assert total <= TOTAL_TOL, (total, worst[:5])
 
 
+@pytest.mark.parametrize("layers,n", [(2, 1500), (8, 4000)])
+def test_rollout_forward_matches_training_forward(gpu, layers, n):
+    """The forward pass without a backward (rollouts: each MLP's second layer runs with its
+    LayerNorm in the GEMM's epilogue) predicts what the training forward (a separate LayerNorm
+    kernel over FP32 rows) predicts, up to BF16 rounding of the normalised rows, and the FP64
+    oracle's predictions within the bound of the gradient test."""
+    p, state, hist, target = scene(n, seed=layers + 20)
+    with Surrogate(layers=layers, seed=7) as s, Fluid("fused", p) as f:
+        w = perturbed_params(s, seed=13)
+        s.set_params(w)
+        f.setup(state)
+        s.sample(f, 1e-3, hist, target)
+        s.forward_backward(True)
+        p_train = s.predictions()
+        s.forward_backward(False)
+        p_roll = s.predictions()
+        xn, xe, recv, send = R.sample_inputs(state, hist, p, s.config.velocity_scale, 1e-3, s.config.accel_scale,
+                                             None, 0)
+        _, _, ref_pred = R.Net(w, layers).loss_and_grads(xn, xe, recv, send, target, s.config.accel_scale)
+    d = np.linalg.norm(p_roll[:, :3] - p_train[:, :3]) / np.linalg.norm(p_train[:, :3])
+    assert d <= 1e-2, d
+    perr = np.linalg.norm(p_roll[:, :3] - ref_pred) / np.linalg.norm(ref_pred)
+    assert perr <= 2e-2, perr
+
+
 def test_gradients_accumulate_and_adam_moves_weights(gpu):
     p, state, hist, target = scene(1200, seed=5)
     with Surrogate(layers=2, seed=3) as s, Fluid("acc", p) as f:
